@@ -1,0 +1,180 @@
+"""Extract the known-answer vectors that pin hmpc's hot path from the
+reference's own Catch2 test sources and write them to reference_kats.json.
+
+The reference cannot be compiled in this environment (it needs a SYCL
+compiler and C++23 deducing-this), so its tests are read as text: every value
+in the JSON is copied from a REQUIRE/CHECK line or a literal in those files,
+and each record carries the file:line it came from.
+
+Usage (in a checkout that has the reference sources):
+    python tests/golden/extract_reference_kats.py /path/to/hmpc
+"""
+import json
+import pathlib
+import re
+import sys
+
+HEX = r"0x[0-9a-fA-F']+"
+
+
+def h(text):
+    return int(text.replace("'", ""), 16)
+
+
+def lines_of(path):
+    return path.read_text().splitlines()
+
+
+def chacha_vectors(root):
+    rel = "tests/crypto/chacha.cpp"
+    src = lines_of(root / rel)
+    out = {"file": rel}
+
+    # quarter round: inputs are declarations, outputs are REQUIREs
+    qr_in, qr_out = {}, {}
+    for no, line in enumerate(src, 1):
+        m = re.search(r"hmpc::core::uint32 ([abcd]) = (" + HEX + r");", line)
+        if m:
+            qr_in[m.group(1)] = (h(m.group(2)), no)
+        m = re.search(r"REQUIRE\(([abcd]) == (" + HEX + r")\);", line)
+        if m:
+            qr_out[m.group(1)] = (h(m.group(2)), no)
+    out["quarter_round"] = {
+        "input": [qr_in[k][0] for k in "abcd"],
+        "output": [qr_out[k][0] for k in "abcd"],
+        "lines": f"{rel}:{qr_in['a'][1]}-{qr_out['d'][1]}",
+    }
+
+    # block function and the additional vectors: replay the section as a tiny
+    # program of array declarations, element assignments, chacha() calls and
+    # REQUIREs on state words.
+    arrays = {}
+    blocks = []
+    current = None
+    pending_state = None
+    calls = 0
+    for no, line in enumerate(src, 1):
+        m = re.search(r"hmpc::core::uint32 (?:const )?(key|nonce|counter)\[\] = \{([^}]*)\};", line)
+        if m:
+            arrays[m.group(1)] = [h(x.strip()) for x in m.group(2).split(",")]
+            calls = 0
+            continue
+        m = re.search(r"\b(key|nonce|counter)\[(\d+)\] = (" + HEX + r");", line)
+        if m:
+            arrays[m.group(1)][int(m.group(2))] = h(m.group(3))
+            continue
+        if "chacha.param({key, nonce, counter});" in line:
+            calls = 0
+            continue
+        if re.search(r"state = chacha\(\);", line):
+            current = {
+                "key": list(arrays["key"]),
+                "nonce": list(arrays["nonce"]),
+                "counter": arrays["counter"][0] + calls,
+                "words": [None] * 16,
+                "line": no,
+            }
+            calls += 1
+            blocks.append(current)
+            continue
+        m = re.search(r"REQUIRE\(state\[(\d+)\] == (" + HEX + r")\);", line)
+        if m and current is not None:
+            current["words"][int(m.group(1))] = h(m.group(2))
+            current["last_line"] = no
+    for b in blocks:
+        assert None not in b["words"], b
+        b["lines"] = f"{rel}:{b.pop('line')}-{b.pop('last_line')}"
+    out["blocks"] = blocks
+    return out
+
+
+def mod_vectors(root):
+    rel = "tests/ints/mod.cpp"
+    src = lines_of(root / rel)
+    text = "\n".join(src)
+    p = h(re.search(r"constexpr auto p = (" + HEX + r")_int;", text).group(1))
+    out = {"file": rel, "p": p}
+    for no, line in enumerate(src, 1):
+        m = re.search(r"reduced_auxiliary_modulus == (" + HEX + r")_int", line)
+        if m:
+            out["R_mod_p"] = {"value": h(m.group(1)), "line": f"{rel}:{no}"}
+        m = re.search(r"auto fivetwelve_montgomery = (" + HEX + r")_int;", line)
+        if m:
+            out["montgomery_512"] = {"value": h(m.group(1)), "line": f"{rel}:{no}"}
+        m = re.search(r"mod_p\((-?)(" + HEX + r")_int\)\) == (" + HEX + r")_int", line)
+        if m:
+            out.setdefault("conversions", []).append({
+                "input_negative": m.group(1) == "-",
+                "input": h(m.group(2)),
+                "canonical": h(m.group(3)),
+                "line": f"{rel}:{no}",
+            })
+    return out
+
+
+def poly_mod_vectors(root):
+    rel = "tests/ints/poly_mod.cpp"
+    src = lines_of(root / rel)
+    text = "\n".join(src)
+    p = h(re.search(r"constexpr auto p = (" + HEX + r")_int;", text).group(1))
+    log_n = int(re.search(r"constexpr hmpc::size N = 1 << (\d+);", text).group(1))
+    out = {"file": rel, "q": p, "N": 1 << log_n, "input": "x_i = i (canonical), every polynomial"}
+    outputs = []
+    for no, line in enumerate(src, 1):
+        m = re.search(r"static_cast<integer>\(y\.root\) == (" + HEX + r")_int", line)
+        if m:
+            out["root"] = {"value": h(m.group(1)), "line": f"{rel}:{no}"}
+        m = re.search(r"static_cast<integer>\(ntt_y\.root\) == (" + HEX + r")_int", line)
+        if m:
+            out["inverse_root"] = {"value": h(m.group(1)), "line": f"{rel}:{no}"}
+        m = re.search(r"index_type\{j, (\d+)\}\]\)\) == (" + HEX + r")_int", line)
+        if m:
+            outputs.append({"index": int(m.group(1)), "canonical": h(m.group(2)), "line": f"{rel}:{no}"})
+    out["ntt_outputs"] = outputs
+    return out
+
+
+def root_of_unity_vectors(root):
+    rel = "tests/ints/num/theory/root_of_unity.cpp"
+    text = (root / rel).read_text()
+    p = int(re.search(r"constexpr auto p = 0b([01']+)_int;", text).group(1).replace("'", ""), 2)
+    log_n = int(re.search(r"constexpr hmpc::size n = 1 << (\d+);", text).group(1))
+    return {"file": rel, "p": p, "degree": 1 << log_n, "property": "root^degree == 1, root^i != 1 for 0 < i < degree"}
+
+
+def lhe_vectors(root):
+    rel = "tests/expr/crypto/lhe/enc.cpp"
+    text = (root / rel).read_text()
+    p = h(re.search(r"constexpr auto p = (" + HEX + r")_int;", text).group(1))
+    q = h(re.search(r"constexpr auto q = (" + HEX + r")_int;", text).group(1))
+    log_n = int(re.search(r"constexpr auto N = hmpc::size\{1\} << (\d+);", text).group(1))
+    shape = [int(x) for x in re.search(r"auto shape = hmpc::shape\{(\d+), (\d+)\};", text).groups()]
+    return {
+        "file": rel,
+        "p": p,
+        "q": q,
+        "N": 1 << log_n,
+        "shape": shape,
+        "key": "a = b = raw Montgomery representative i; s = Montgomery one",
+        "plaintext": "NTT_p representation, raw representative i",
+        "property": "dec(s, enc(key, x, randomness)) == x",
+    }
+
+
+def main():
+    root = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    data = {
+        "source": "hmpc v0.5.2 Catch2 tests, read as text",
+        "chacha20": chacha_vectors(root),
+        "mod": mod_vectors(root),
+        "poly_mod_ntt": poly_mod_vectors(root),
+        "root_of_unity": root_of_unity_vectors(root),
+        "linear_bgv": lhe_vectors(root),
+    }
+    out = pathlib.Path(__file__).with_name("reference_kats.json")
+    out.write_text(json.dumps(data, indent=1, default=str) + "\n")
+    print(f"wrote {out}")
+
+
+if __name__ == "__main__":
+    main()
