@@ -1,0 +1,247 @@
+"""Device-side objects that mirror hmpc::comp: the queue (one GPU, its stream
+and the RNG capability), moduli, and limb-planar tensors.
+
+Reference interfaces: hmpc/comp/queue.hpp:163-599 (queue), hmpc/comp/tensor.hpp
+:9-90 (tensor, make_tensor), hmpc/ints/mod.hpp:73-193 (mod<Q>).  Every
+operation runs through the C ABI of libhmpc_gb300.so; PyTorch only provides
+device memory and the stream.
+"""
+import ctypes
+import os
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def _words(value, n=None):
+    value = int(value)
+    n = n or max(1, (value.bit_length() + 31) // 32)
+    return [(value >> (32 * i)) & 0xFFFFFFFF for i in range(n)]
+
+
+def _u32_array(values):
+    return (ctypes.c_uint32 * len(values))(*values)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+class Modulus:
+    """mod<Q> registered on a queue: L, bit width and Montgomery one
+    (hmpc/ints/mod.hpp:90-127).  Twiddle tables per ring degree are cached on
+    the device (hmpc/comp/queue.hpp:364-381)."""
+
+    def __init__(self, queue, q):
+        self.queue = queue
+        self.value = int(q)
+        handle = ctypes.c_void_p()
+        words = _words(self.value)
+        _lib.call("hmpc_modulus_create", queue.handle, _u32_array(words), len(words), ctypes.byref(handle))
+        self.handle = handle
+        limbs, bits = ctypes.c_int(), ctypes.c_int()
+        one = (ctypes.c_uint32 * 16)()
+        _lib.call("hmpc_modulus_info", handle, ctypes.byref(limbs), ctypes.byref(bits), one)
+        self.limbs = limbs.value
+        self.bits = bits.value
+        self.one = sum(int(one[i]) << (32 * i) for i in range(self.limbs))
+
+    def prepare(self, n):
+        _lib.call("hmpc_modulus_prepare", self.handle, n)
+
+    def root(self, n, inverse=False):
+        out = (ctypes.c_uint32 * 16)()
+        _lib.call("hmpc_modulus_root", self.handle, n, int(inverse), out)
+        return sum(int(out[i]) << (32 * i) for i in range(self.limbs))
+
+    def twiddles(self, n, inverse=False):
+        table = np.zeros(n * self.limbs, dtype=np.uint32)
+        _lib.call("hmpc_modulus_twiddles", self.handle, n, int(inverse),
+                  table.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        return table.reshape(n, self.limbs)
+
+    def __repr__(self):
+        return f"Modulus({self.value:#x}, limbs={self.limbs})"
+
+
+class Tensor:
+    """comp::tensor<T, Dimensions...>: limb-planar device storage
+    [limbs][elements] (hmpc/comp/tensor.hpp:21,25-29).  `shape` is the batch
+    shape and `n` the polynomial degree (1 for plain residues), so elements =
+    prod(shape) * n in (batch..., coefficient) row-major order."""
+
+    def __init__(self, modulus, shape, n=1, data=None):
+        self.modulus = modulus
+        self.shape = tuple(int(s) for s in shape)
+        self.n = int(n)
+        self.elements = int(np.prod(self.shape, dtype=np.int64)) * self.n
+        if data is None:
+            data = torch.empty((modulus.limbs, self.elements), dtype=torch.int32, device=modulus.queue.device)
+        assert data.dtype == torch.int32 and data.shape == (modulus.limbs, self.elements) and data.is_contiguous()
+        self.data = data
+
+    @property
+    def batch(self):
+        return int(np.prod(self.shape, dtype=np.int64))
+
+    def numpy(self):
+        return self.data.cpu().numpy().view(np.uint32)
+
+    @classmethod
+    def from_numpy(cls, modulus, array, shape, n=1):
+        array = np.ascontiguousarray(array, dtype=np.uint32)
+        data = torch.from_numpy(array.view(np.int32)).to(modulus.queue.device)
+        return cls(modulus, shape, n, data.contiguous())
+
+    def ptr(self):
+        return _ptr(self.data)
+
+
+def make_tensor(modulus, shape, n=1):
+    """hmpc::comp::make_tensor<T>(shape) (hmpc/comp/tensor.hpp:86-90)"""
+    return Tensor(modulus, shape, n)
+
+
+class Queue:
+    """hmpc::comp::queue on one GPU: the stream, the 8-word ChaCha20 key and
+    the 96-bit nonce of the RNG capability (hmpc/comp/queue.hpp:175-253)."""
+
+    def __init__(self, key=None, device=0, stream=None):
+        self.device = torch.device("cuda", device)
+        if key is None:
+            key = list(np.frombuffer(os.urandom(32), dtype=np.uint32))  # queue.hpp:229-233
+        self.key = [int(k) & 0xFFFFFFFF for k in key]
+        self.stream = stream if stream is not None else torch.cuda.current_stream(self.device)
+        handle = ctypes.c_void_p()
+        _lib.call("hmpc_context_create", device, _u32_array(self.key), ctypes.c_void_p(self.stream.cuda_stream),
+                  ctypes.byref(handle))
+        self.handle = handle
+        self._moduli = {}
+
+    def close(self):
+        if self.handle:
+            _lib.call("hmpc_context_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        self.stream = stream
+        _lib.call("hmpc_context_set_stream", self.handle, ctypes.c_void_p(stream.cuda_stream))
+
+    @property
+    def nonce(self):
+        out = (ctypes.c_uint32 * 3)()
+        _lib.call("hmpc_context_get_nonce", self.handle, out)
+        return [int(x) for x in out]
+
+    @nonce.setter
+    def nonce(self, value):
+        _lib.call("hmpc_context_set_nonce", self.handle, _u32_array([int(v) & 0xFFFFFFFF for v in value]))
+
+    @property
+    def launches(self):
+        """kernels launched through this queue so far"""
+        out = ctypes.c_uint64()
+        _lib.call("hmpc_context_launch_count", self.handle, ctypes.byref(out))
+        return out.value
+
+    def int_multiply_rate(self):
+        """measured 32-bit multiply operations per second of the device"""
+        out = ctypes.c_double()
+        _lib.call("hmpc_probe_int_multiply_rate", self.handle, ctypes.byref(out))
+        return out.value
+
+    def wait(self):
+        """queue.wait() (hmpc/comp/queue.hpp:531-534)"""
+        _lib.call("hmpc_context_synchronize", self.handle)
+
+    def modulus(self, q):
+        q = int(q)
+        if q not in self._moduli:
+            self._moduli[q] = Modulus(self, q)
+        return self._moduli[q]
+
+    # ------------------------------------------------------------ transforms
+    def ntt(self, x, out=None):
+        """number_theoretic_transform(tensor(x))"""
+        out = out or make_tensor(x.modulus, x.shape, x.n)
+        prod = _lib.Producer(_lib.PRODUCER_TENSOR, x.data.data_ptr(), 0, 0)
+        _lib.call("hmpc_ntt_forward", self.handle, x.modulus.handle, x.n, x.batch, ctypes.byref(prod), out.ptr())
+        return out
+
+    def intt(self, x, out=None):
+        """inverse_number_theoretic_transform(tensor(x))"""
+        out = out or make_tensor(x.modulus, x.shape, x.n)
+        _lib.call("hmpc_ntt_inverse", self.handle, x.modulus.handle, x.n, x.batch, x.ptr(), out.ptr())
+        return out
+
+    def ntt_centered_binomial(self, modulus, n, shape, variance_x2, out=None):
+        """number_theoretic_transform(centered_binomial<R>(shape, V)), 2V = variance_x2;
+        the sampler runs inside the transform's first pass."""
+        out = out or make_tensor(modulus, shape, n)
+        prod = _lib.Producer(_lib.PRODUCER_CBD, None, variance_x2, 0)
+        _lib.call("hmpc_ntt_forward", self.handle, modulus.handle, n, out.batch, ctypes.byref(prod), out.ptr())
+        return out
+
+    def ntt_uniform(self, modulus, n, shape, security=80, out=None):
+        """number_theoretic_transform(uniform<R>(shape))"""
+        out = out or make_tensor(modulus, shape, n)
+        prod = _lib.Producer(_lib.PRODUCER_UNIFORM, None, 0, security)
+        _lib.call("hmpc_ntt_forward", self.handle, modulus.handle, n, out.batch, ctypes.byref(prod), out.ptr())
+        return out
+
+    # ----------------------------------------------------------- elementwise
+    def fma(self, a, b, c, out=None):
+        out = out or make_tensor(a.modulus, a.shape, a.n)
+        _lib.call("hmpc_fma", self.handle, a.modulus.handle, a.elements, a.ptr(), b.ptr(), c.ptr(), out.ptr())
+        return out
+
+    def binary(self, op, a, b, out=None):
+        big = a if a.elements >= b.elements else b
+        out = out or make_tensor(big.modulus, big.shape, big.n)
+        _lib.call("hmpc_binary", self.handle, big.modulus.handle, op, out.elements, a.ptr(), a.elements, b.ptr(),
+                  b.elements, out.ptr())
+        return out
+
+    def add(self, a, b, out=None):
+        return self.binary(_lib.OP_ADD, a, b, out)
+
+    def sub(self, a, b, out=None):
+        return self.binary(_lib.OP_SUB, a, b, out)
+
+    def mul(self, a, b, out=None):
+        return self.binary(_lib.OP_MUL, a, b, out)
+
+    def uniform(self, modulus, shape, n=1, security=80, out=None):
+        """uniform<T>(shape) evaluated elementwise (expr/random/uniform.hpp:11-46)"""
+        out = out or make_tensor(modulus, shape, n)
+        _lib.call("hmpc_sample_uniform", self.handle, modulus.handle, out.elements, security, out.ptr())
+        return out
+
+    def centered_binomial(self, modulus, shape, variance_x2, n=1, out=None):
+        out = out or make_tensor(modulus, shape, n)
+        _lib.call("hmpc_sample_cbd", self.handle, modulus.handle, out.elements, variance_x2, out.ptr())
+        return out
+
+    def cast(self, x, modulus, out=None):
+        """cast<mod<Q'>>(x): centred lift (hmpc/ints/mod.hpp:259-307)"""
+        out = out or make_tensor(modulus, x.shape, x.n)
+        _lib.call("hmpc_cast", self.handle, modulus.handle, x.modulus.handle, x.elements, x.ptr(), out.ptr())
+        return out
+
+    def to_montgomery(self, x, out=None):
+        out = out or make_tensor(x.modulus, x.shape, x.n)
+        _lib.call("hmpc_to_montgomery", self.handle, x.modulus.handle, x.elements, x.ptr(), out.ptr())
+        return out
+
+    def from_montgomery(self, x, out=None):
+        out = out or make_tensor(x.modulus, x.shape, x.n)
+        _lib.call("hmpc_from_montgomery", self.handle, x.modulus.handle, x.elements, x.ptr(), out.ptr())
+        return out

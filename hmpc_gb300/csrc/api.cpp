@@ -1,0 +1,955 @@
+// C-ABI layer: contexts (device, stream, RNG capability), registered moduli
+// with their cached twiddle tables, the NTT pass planner and the launchers.
+#include "../../include/hmpc_gb300.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "dispatch.hpp"
+#include "host_math.hpp"
+#include "plan.hpp"
+#include "probe.hpp"
+
+using namespace hmpc_gb300;
+
+namespace
+{
+    thread_local std::string last_error;
+
+    int fail(int code, const std::string& message)
+    {
+        last_error = message;
+        return code;
+    }
+
+    int cuda_fail(cudaError_t e, const char* what)
+    {
+        return fail(HMPC_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+
+#define HMPC_CUDA(call, what)                                                                                         \
+    do                                                                                                                \
+    {                                                                                                                 \
+        cudaError_t hmpc_e_ = (call);                                                                                 \
+        if (hmpc_e_ != cudaSuccess)                                                                                   \
+        {                                                                                                             \
+            return cuda_fail(hmpc_e_, what);                                                                          \
+        }                                                                                                             \
+    } while (0)
+
+    host::words to_words(const uint32_t* p, int n)
+    {
+        return host::words(p, p + n);
+    }
+
+    void nonce_add(uint32_t nonce[3], uint64_t v)
+    {
+        uint64_t s = static_cast<uint64_t>(nonce[0]) + static_cast<uint32_t>(v);
+        nonce[0] = static_cast<uint32_t>(s);
+        s = static_cast<uint64_t>(nonce[1]) + static_cast<uint32_t>(v >> 32) + (s >> 32);
+        nonce[1] = static_cast<uint32_t>(s);
+        nonce[2] += static_cast<uint32_t>(s >> 32);
+    }
+
+    struct Tables
+    {
+        uint32_t* forward = nullptr;
+        uint32_t* inverse = nullptr;
+        host::words root, inverse_root;
+    };
+}
+
+struct hmpc_context
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t key[8] = {};
+    uint32_t nonce[3] = {};
+    uint32_t* workspace = nullptr;
+    uint64_t workspace_words = 0;
+    uint64_t launches = 0;  // kernels launched through this context
+    std::vector<hmpc_modulus*> moduli;
+
+    uint32_t* scratch(uint64_t words)
+    {
+        if (words > workspace_words)
+        {
+            if (workspace)
+            {
+                cudaStreamSynchronize(stream);
+                cudaFree(workspace);
+                workspace = nullptr;
+                workspace_words = 0;
+            }
+            if (cudaMalloc(&workspace, words * sizeof(uint32_t)) != cudaSuccess)
+            {
+                return nullptr;
+            }
+            workspace_words = words;
+        }
+        return workspace;
+    }
+
+    RngKey rng() const
+    {
+        RngKey k{};
+        std::memcpy(k.key, key, sizeof key);
+        std::memcpy(k.nonce, nonce, sizeof nonce);
+        return k;
+    }
+};
+
+struct hmpc_modulus
+{
+    hmpc_context* ctx = nullptr;
+    host::ModulusConstants c;
+    HostModulus h;
+    const KernelTable* kt = nullptr;
+    uint32_t* small_table = nullptr;  // Montgomery forms of 0..64, element-major
+    std::map<uint64_t, Tables> tables;
+
+    ~hmpc_modulus()
+    {
+        cudaFree(small_table);
+        for (auto& kv : tables)
+        {
+            cudaFree(kv.second.forward);
+            cudaFree(kv.second.inverse);
+        }
+    }
+
+    int prepare(uint64_t n, Tables** out)
+    {
+        auto it = tables.find(n);
+        if (it == tables.end())
+        {
+            Tables t;
+            std::vector<uint32_t> fwd, inv;
+            std::string error;
+            if (!host::twiddle_table(c, n, false, fwd, t.root, error) ||
+                !host::twiddle_table(c, n, true, inv, t.inverse_root, error))
+            {
+                return fail(HMPC_ERROR_NO_ROOT, error);
+            }
+            const size_t bytes = fwd.size() * sizeof(uint32_t);
+            HMPC_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+            HMPC_CUDA(cudaMalloc(&t.forward, bytes), "allocating twiddles");
+            if (cudaMalloc(&t.inverse, bytes) != cudaSuccess)
+            {
+                cudaFree(t.forward);
+                return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating twiddles");
+            }
+            HMPC_CUDA(cudaMemcpy(t.forward, fwd.data(), bytes, cudaMemcpyHostToDevice), "uploading twiddles");
+            HMPC_CUDA(cudaMemcpy(t.inverse, inv.data(), bytes, cudaMemcpyHostToDevice), "uploading twiddles");
+            it = tables.emplace(n, t).first;
+        }
+        if (out)
+        {
+            *out = &it->second;
+        }
+        return HMPC_OK;
+    }
+};
+
+namespace
+{
+    int check_degree(uint64_t n)
+    {
+        if (n < 4 || (n & (n - 1)) != 0 || n > (1ull << 30))
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "ring degree must be a power of two in [4, 2^30]");
+        }
+        return HMPC_OK;
+    }
+
+    int enter(hmpc_context* ctx)
+    {
+        if (!ctx)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null context");
+        }
+        HMPC_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+        return HMPC_OK;
+    }
+
+    int run_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
+                      uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out)
+    {
+        if (int rc = enter(ctx))
+        {
+            return rc;
+        }
+        if (!mod || !out)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus or output");
+        }
+        if (int rc = check_degree(n))
+        {
+            return rc;
+        }
+        if (batch == 0)
+        {
+            return HMPC_OK;
+        }
+        Tables* t = nullptr;
+        if (int rc = mod->prepare(n, &t))
+        {
+            return rc;
+        }
+        const int L = mod->c.limbs;
+        int nw = 1;
+        uint32_t top_mask = 0xffffffffu;
+        if (kind == producer_cbd)
+        {
+            if (vx2 < 1 || vx2 > 64)
+            {
+                return fail(HMPC_ERROR_UNSUPPORTED, "centred binomial needs 1 <= 2V <= 64");
+            }
+            nw = static_cast<int>((2 * vx2 + 31) / 32);
+        }
+        else if (kind == producer_uniform)
+        {
+            const uint32_t bits = static_cast<uint32_t>(mod->c.bits) + security;
+            nw = static_cast<int>((bits + 31) / 32);
+            if (nw != L + 2 && nw != L + 3)
+            {
+                return fail(HMPC_ERROR_UNSUPPORTED, "uniform sampler supports statistical security 80");
+            }
+            if (bits % 32)
+            {
+                top_mask = (1u << (bits % 32)) - 1u;
+            }
+        }
+        else if (kind != producer_tensor)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "unknown producer kind");
+        }
+        if (kind == producer_tensor && !src)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "tensor producer without source");
+        }
+        const int log_n = __builtin_ctzll(n);
+        const std::vector<PassPlan> plan = plan_transform(L, log_n, batch, inverse, mod->kt->radix_bits);
+        const RngKey rng = ctx->rng();
+        for (size_t i = 0; i < plan.size(); ++i)
+        {
+            NttPassParams p = plan[i].params;
+            p.out = out;
+            p.src = i == 0 ? src : nullptr;
+            p.twiddles = inverse ? t->inverse : t->forward;
+            p.small_table = mod->small_table;
+            p.elements = n * batch;
+            p.rng = rng;
+            p.vx2 = vx2;
+            p.top_mask = top_mask;
+            const int k = i == 0 ? kind : producer_tensor;
+            cudaError_t e = mod->kt->ntt_pass(p, k, k == producer_tensor ? 1 : nw, mod->h, plan[i].grid,
+                                              plan[i].block, plan[i].smem, ctx->stream);
+            if (e != cudaSuccess)
+            {
+                return cuda_fail(e, "launching NTT pass");
+            }
+            ++ctx->launches;
+        }
+        if (kind != producer_tensor)
+        {
+            nonce_add(ctx->nonce, n * batch);
+        }
+        return HMPC_OK;
+    }
+
+    CastParams make_cast(const hmpc_modulus* dst, const hmpc_modulus* src)
+    {
+        CastParams cp{};
+        const int ls = src->c.limbs;
+        const int ld = dst->c.limbs;
+        cp.src_limbs = static_cast<uint32_t>(ls);
+        cp.src_ninv = src->c.ninv;
+        for (int j = 0; j < ls; ++j)
+        {
+            cp.src_q[j] = src->c.q[static_cast<size_t>(j)];
+            cp.src_half[j] = src->c.half[static_cast<size_t>(j)];
+        }
+        const int nw = std::max(ls, ld) + 1;
+        cp.norm_words = static_cast<uint32_t>(nw);
+        host::words offset;
+        if (host::compare(dst->c.q, src->c.q) > 0)
+        {
+            offset = host::sub(dst->c.q, src->c.q, nw);
+            cp.direct = 1;
+            for (int j = 0; j < ld; ++j)
+            {
+                cp.factor[j] = dst->c.r2[static_cast<size_t>(j)];
+            }
+        }
+        else
+        {
+            const host::words rem = host::mod(src->c.q, dst->c.q);
+            offset = host::bit_width(rem) == 0 ? host::words(static_cast<size_t>(nw), 0u) : host::sub(dst->c.q, rem, nw);
+            cp.direct = 0;
+            host::words wide(static_cast<size_t>(nw + ld), 0u);
+            for (int j = 0; j < ld; ++j)
+            {
+                wide[static_cast<size_t>(nw + j)] = dst->c.r2[static_cast<size_t>(j)];
+            }
+            const host::words f = host::mod(wide, dst->c.q);
+            for (int j = 0; j < ld; ++j)
+            {
+                cp.factor[j] = f[static_cast<size_t>(j)];
+            }
+        }
+        offset = host::resize(offset, nw);
+        for (int j = 0; j < nw; ++j)
+        {
+            cp.offset[j] = offset[static_cast<size_t>(j)];
+        }
+        return cp;
+    }
+}
+
+extern "C" {
+
+const char* hmpc_last_error(void)
+{
+    return last_error.c_str();
+}
+
+int hmpc_version(int* major, int* minor)
+{
+    if (major)
+    {
+        *major = 0;
+    }
+    if (minor)
+    {
+        *minor = 1;
+    }
+    return HMPC_OK;
+}
+
+int hmpc_context_create(int device, const uint32_t key[8], void* stream, hmpc_context** out)
+{
+    if (!out)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
+    }
+    int count = 0;
+    HMPC_CUDA(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (device < 0 || device >= count)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "no such CUDA device");
+    }
+    HMPC_CUDA(cudaSetDevice(device), "cudaSetDevice");
+    auto* ctx = new hmpc_context;
+    ctx->device = device;
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    if (key)
+    {
+        std::memcpy(ctx->key, key, sizeof ctx->key);
+    }
+    *out = ctx;
+    return HMPC_OK;
+}
+
+int hmpc_context_destroy(hmpc_context* ctx)
+{
+    if (!ctx)
+    {
+        return HMPC_OK;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto* m : ctx->moduli)
+    {
+        delete m;
+    }
+    cudaFree(ctx->workspace);
+    delete ctx;
+    return HMPC_OK;
+}
+
+int hmpc_context_set_stream(hmpc_context* ctx, void* stream)
+{
+    if (!ctx)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null context");
+    }
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    return HMPC_OK;
+}
+
+int hmpc_context_get_nonce(const hmpc_context* ctx, uint32_t nonce[3])
+{
+    if (!ctx || !nonce)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    std::memcpy(nonce, ctx->nonce, sizeof ctx->nonce);
+    return HMPC_OK;
+}
+
+int hmpc_context_set_nonce(hmpc_context* ctx, const uint32_t nonce[3])
+{
+    if (!ctx || !nonce)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    std::memcpy(ctx->nonce, nonce, sizeof ctx->nonce);
+    return HMPC_OK;
+}
+
+int hmpc_context_launch_count(const hmpc_context* ctx, uint64_t* count)
+{
+    if (!ctx || !count)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    *count = ctx->launches;
+    return HMPC_OK;
+}
+
+int hmpc_probe_int_multiply_rate(hmpc_context* ctx, double* ops_per_second)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!ops_per_second)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
+    }
+    cudaError_t e = probe_int_multiply_rate(ctx->stream, ops_per_second);
+    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "integer multiply probe");
+}
+
+int hmpc_context_synchronize(hmpc_context* ctx)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    HMPC_CUDA(cudaStreamSynchronize(ctx->stream), "synchronizing");
+    return HMPC_OK;
+}
+
+int hmpc_modulus_create(hmpc_context* ctx, const uint32_t* q, int q_words, hmpc_modulus** out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!q || q_words <= 0 || !out)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus words");
+    }
+    auto m = std::make_unique<hmpc_modulus>();
+    std::string error;
+    if (!host::make_constants(to_words(q, q_words), m->c, error))
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, error);
+    }
+    const int L = m->c.limbs;
+    if (L > max_device_limbs)
+    {
+        return fail(HMPC_ERROR_UNSUPPORTED, "moduli up to 9 limbs (288 bits) are supported on the device");
+    }
+    m->ctx = ctx;
+    m->kt = kernel_table(L);
+    m->h.limbs = L;
+    m->h.bits = m->c.bits;
+    m->h.ninv = m->c.ninv;
+    for (int j = 0; j < L; ++j)
+    {
+        m->h.q[j] = m->c.q[static_cast<size_t>(j)];
+        m->h.one[j] = m->c.one[static_cast<size_t>(j)];
+        m->h.r2[j] = m->c.r2[static_cast<size_t>(j)];
+        m->h.half[j] = m->c.half[static_cast<size_t>(j)];
+    }
+    std::vector<uint32_t> small(static_cast<size_t>(65 * L));
+    for (uint32_t v = 0; v <= 64; ++v)
+    {
+        const host::words mv = host::to_mont(m->c, host::words{v});
+        std::copy(mv.begin(), mv.end(), small.begin() + static_cast<std::ptrdiff_t>(v * static_cast<uint32_t>(L)));
+    }
+    HMPC_CUDA(cudaMalloc(&m->small_table, small.size() * sizeof(uint32_t)), "allocating constants");
+    HMPC_CUDA(cudaMemcpy(m->small_table, small.data(), small.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+              "uploading constants");
+    ctx->moduli.push_back(m.get());
+    *out = m.release();
+    return HMPC_OK;
+}
+
+int hmpc_modulus_destroy(hmpc_modulus* mod)
+{
+    if (!mod)
+    {
+        return HMPC_OK;
+    }
+    auto& list = mod->ctx->moduli;
+    list.erase(std::remove(list.begin(), list.end(), mod), list.end());
+    cudaSetDevice(mod->ctx->device);
+    cudaStreamSynchronize(mod->ctx->stream);
+    delete mod;
+    return HMPC_OK;
+}
+
+int hmpc_modulus_info(const hmpc_modulus* mod, int* limbs, int* bits, uint32_t* one)
+{
+    if (!mod)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
+    }
+    if (limbs)
+    {
+        *limbs = mod->c.limbs;
+    }
+    if (bits)
+    {
+        *bits = mod->c.bits;
+    }
+    if (one)
+    {
+        std::copy(mod->c.one.begin(), mod->c.one.end(), one);
+    }
+    return HMPC_OK;
+}
+
+int hmpc_modulus_prepare(hmpc_modulus* mod, uint64_t n)
+{
+    if (!mod)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    return mod->prepare(n, nullptr);
+}
+
+int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root)
+{
+    if (!mod || !root)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    Tables* t = nullptr;
+    if (int rc = mod->prepare(n, &t))
+    {
+        return rc;
+    }
+    const host::words& r = inverse ? t->inverse_root : t->root;
+    std::copy(r.begin(), r.end(), root);
+    return HMPC_OK;
+}
+
+int hmpc_modulus_twiddles(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* host_table)
+{
+    if (!mod || !host_table)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    Tables* t = nullptr;
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    if (int rc = mod->prepare(n, &t))
+    {
+        return rc;
+    }
+    HMPC_CUDA(cudaMemcpy(host_table, inverse ? t->inverse : t->forward,
+                         n * static_cast<uint64_t>(mod->c.limbs) * sizeof(uint32_t), cudaMemcpyDeviceToHost),
+              "downloading twiddles");
+    return HMPC_OK;
+}
+
+int hmpc_tensor_alloc(hmpc_context* ctx, uint64_t words, uint32_t** out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!out)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
+    }
+    if (cudaMalloc(out, std::max<uint64_t>(words, 1) * sizeof(uint32_t)) != cudaSuccess)
+    {
+        return fail(HMPC_ERROR_OUT_OF_MEMORY, "cudaMalloc failed");
+    }
+    return HMPC_OK;
+}
+
+int hmpc_tensor_free(hmpc_context* ctx, uint32_t* ptr)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    HMPC_CUDA(cudaFree(ptr), "cudaFree");
+    return HMPC_OK;
+}
+
+int hmpc_tensor_upload(hmpc_context* ctx, uint32_t* dst, const uint32_t* host, uint64_t words)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    HMPC_CUDA(cudaMemcpyAsync(dst, host, words * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream), "upload");
+    return HMPC_OK;
+}
+
+int hmpc_tensor_download(hmpc_context* ctx, uint32_t* host, const uint32_t* src, uint64_t words)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    HMPC_CUDA(cudaMemcpyAsync(host, src, words * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream),
+              "download");
+    HMPC_CUDA(cudaStreamSynchronize(ctx->stream), "download");
+    return HMPC_OK;
+}
+
+int hmpc_ntt_forward(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const hmpc_producer* producer,
+                     uint32_t* out)
+{
+    if (!producer)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null producer");
+    }
+    return run_transform(ctx, mod, n, batch, false, producer->kind, producer->variance_x2, producer->security,
+                         producer->src, out);
+}
+
+int hmpc_ntt_inverse(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const uint32_t* in,
+                     uint32_t* out)
+{
+    return run_transform(ctx, mod, n, batch, true, producer_tensor, 0, 0, in, out);
+}
+
+int hmpc_fma(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* a, const uint32_t* b,
+             const uint32_t* c, uint32_t* d)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!mod || (elements && (!a || !b || !c || !d)))
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    cudaError_t e = mod->kt->fma(d, a, b, c, elements, mod->h, ctx->stream);
+    ctx->launches += elements ? 1 : 0;
+    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "launching fma");
+}
+
+int hmpc_binary(hmpc_context* ctx, hmpc_modulus* mod, int op, uint64_t elements, const uint32_t* a,
+                uint64_t a_elements, const uint32_t* b, uint64_t b_elements, uint32_t* out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!mod || op < 0 || op > 2)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "bad modulus or operation");
+    }
+    if (elements == 0)
+    {
+        return HMPC_OK;
+    }
+    if (!a || !b || !out || a_elements == 0 || b_elements == 0 || elements % a_elements || elements % b_elements)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "operand sizes must divide the result size");
+    }
+    cudaError_t e = mod->kt->binary(out, a, a_elements, b, b_elements, elements, op, mod->h, ctx->stream);
+    ++ctx->launches;
+    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "launching binary op");
+}
+
+int hmpc_sample_uniform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, uint32_t security, uint32_t* out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!mod || (elements && !out))
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    const uint32_t bits = static_cast<uint32_t>(mod->c.bits) + security;
+    const int words = static_cast<int>((bits + 31) / 32);
+    if (words != mod->c.limbs + 2 && words != mod->c.limbs + 3)
+    {
+        return fail(HMPC_ERROR_UNSUPPORTED, "uniform sampler supports statistical security 80");
+    }
+    const uint32_t top_mask = bits % 32 ? (1u << (bits % 32)) - 1u : 0xffffffffu;
+    cudaError_t e = mod->kt->uniform(out, elements, ctx->rng(), words, top_mask, mod->h, ctx->stream);
+    ctx->launches += elements ? 1 : 0;
+    if (e != cudaSuccess)
+    {
+        return cuda_fail(e, "launching uniform sampler");
+    }
+    nonce_add(ctx->nonce, elements);
+    return HMPC_OK;
+}
+
+int hmpc_sample_cbd(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, uint32_t variance_x2, uint32_t* out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!mod || (elements && !out))
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (variance_x2 < 1 || variance_x2 > 64)
+    {
+        return fail(HMPC_ERROR_UNSUPPORTED, "centred binomial needs 1 <= 2V <= 64");
+    }
+    cudaError_t e = mod->kt->cbd(out, elements, ctx->rng(), variance_x2, mod->small_table, mod->h, ctx->stream);
+    ctx->launches += elements ? 1 : 0;
+    if (e != cudaSuccess)
+    {
+        return cuda_fail(e, "launching binomial sampler");
+    }
+    nonce_add(ctx->nonce, elements);
+    return HMPC_OK;
+}
+
+int hmpc_cast(hmpc_context* ctx, hmpc_modulus* dst, hmpc_modulus* src, uint64_t elements, const uint32_t* in,
+              uint32_t* out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!dst || !src || (elements && (!in || !out)))
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    cudaError_t e = dst->kt->cast(out, in, elements, make_cast(dst, src), dst->h, ctx->stream);
+    ctx->launches += elements ? 1 : 0;
+    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "launching cast");
+}
+
+int hmpc_to_montgomery(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* in, uint32_t* out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!mod)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
+    }
+    cudaError_t e = mod->kt->to_montgomery(out, in, elements, mod->h, ctx->stream);
+    ctx->launches += elements ? 1 : 0;
+    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "launching conversion");
+}
+
+int hmpc_from_montgomery(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* in, uint32_t* out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!mod)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
+    }
+    cudaError_t e = mod->kt->from_montgomery(out, in, elements, mod->h, ctx->stream);
+    ctx->launches += elements ? 1 : 0;
+    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "launching conversion");
+}
+
+int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
+                 const uint32_t* key_a, const uint32_t* key_b, const uint32_t* plaintext, int plaintext_ntt,
+                 uint32_t* c0, uint32_t* c1)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!q || !p || !key_a || !key_b || !plaintext || !c0 || !c1)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    if (batch == 0)
+    {
+        return HMPC_OK;
+    }
+    const uint64_t elements = n * batch;
+    const uint64_t lq = static_cast<uint64_t>(q->c.limbs);
+    const uint64_t lp = static_cast<uint64_t>(p->c.limbs);
+    const uint64_t poly_words = elements * lq;
+    uint32_t* ws = ctx->scratch(3 * poly_words + (plaintext_ntt ? elements * lp : 0));
+    if (!ws)
+    {
+        return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating the encryption workspace");
+    }
+    uint32_t* u = ws;
+    uint32_t* v = ws + poly_words;
+    uint32_t* msg = ws + 2 * poly_words;
+    uint32_t* coeff = ws + 3 * poly_words;
+    // the execution order of the reference's plan: NTT(u), NTT(v),
+    // [INTT_p(x)], NTT_q(msg), c0, NTT(w), c1 (expr/cache.hpp:226-271)
+    int rc = run_transform(ctx, q, n, batch, false, producer_cbd, 1, 0, nullptr, u);
+    if (!rc)
+    {
+        rc = run_transform(ctx, q, n, batch, false, producer_cbd, 20, 0, nullptr, v);
+    }
+    const uint32_t* coefficients = plaintext;
+    if (!rc && plaintext_ntt)
+    {
+        rc = run_transform(ctx, p, n, batch, true, producer_tensor, 0, 0, plaintext, coeff);
+        coefficients = coeff;
+    }
+    if (!rc)
+    {
+        cudaError_t e = q->kt->cast(msg, coefficients, elements, make_cast(q, p), q->h, ctx->stream);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "launching cast");
+        }
+        ++ctx->launches;
+        rc = run_transform(ctx, q, n, batch, false, producer_tensor, 0, 0, msg, msg);
+    }
+    const host::words pm = host::to_mont(q->c, p->c.q);
+    if (!rc)
+    {
+        cudaError_t e = q->kt->lhe_combine(c0, key_a, n, u, v, msg, elements, pm.data(), q->h, ctx->stream);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "launching combine");
+        }
+        ++ctx->launches;
+        rc = run_transform(ctx, q, n, batch, false, producer_cbd, 20, 0, nullptr, v);  // w reuses v's buffer
+    }
+    if (!rc)
+    {
+        cudaError_t e = q->kt->lhe_combine(c1, key_b, n, u, v, nullptr, elements, pm.data(), q->h, ctx->stream);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "launching combine");
+        }
+        ++ctx->launches;
+    }
+    return rc;
+}
+
+int hmpc_lhe_dec(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
+                 const uint32_t* s, const uint32_t* c0, const uint32_t* c1, int plaintext_ntt, uint32_t* out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!q || !p || !s || !c0 || !c1 || !out)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    if (batch == 0)
+    {
+        return HMPC_OK;
+    }
+    const uint64_t elements = n * batch;
+    uint32_t* x = ctx->scratch(elements * static_cast<uint64_t>(q->c.limbs));
+    if (!x)
+    {
+        return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating the decryption workspace");
+    }
+    cudaError_t e = q->kt->binary(x, s, n, c1, elements, elements, HMPC_OP_MUL, q->h, ctx->stream);
+    if (e == cudaSuccess)
+    {
+        e = q->kt->binary(x, c0, elements, x, elements, elements, HMPC_OP_SUB, q->h, ctx->stream);
+    }
+    if (e != cudaSuccess)
+    {
+        return cuda_fail(e, "launching elementwise op");
+    }
+    ctx->launches += 2;
+    int rc = run_transform(ctx, q, n, batch, true, producer_tensor, 0, 0, x, x);
+    if (rc)
+    {
+        return rc;
+    }
+    e = p->kt->cast(out, x, elements, make_cast(p, q), p->h, ctx->stream);
+    if (e != cudaSuccess)
+    {
+        return cuda_fail(e, "launching cast");
+    }
+    ++ctx->launches;
+    if (plaintext_ntt)
+    {
+        rc = run_transform(ctx, p, n, batch, false, producer_tensor, 0, 0, out, out);
+    }
+    return rc;
+}
+
+int hmpc_lhe_keygen(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint32_t* s, uint32_t* a,
+                    uint32_t* b)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!q || !p || !s || !a || !b)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    uint32_t* e_poly = ctx->scratch(n * static_cast<uint64_t>(q->c.limbs));
+    if (!e_poly)
+    {
+        return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating the key workspace");
+    }
+    int rc = hmpc_sample_uniform(ctx, q, n, 80, b);
+    if (!rc)
+    {
+        rc = run_transform(ctx, q, n, 1, false, producer_cbd, 1, 0, nullptr, s);
+    }
+    if (!rc)
+    {
+        rc = run_transform(ctx, q, n, 1, false, producer_cbd, 20, 0, nullptr, e_poly);
+    }
+    if (!rc)
+    {
+        const host::words pm = host::to_mont(q->c, p->c.q);
+        cudaError_t e = q->kt->lhe_combine(a, b, n, s, e_poly, nullptr, n, pm.data(), q->h, ctx->stream);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "launching combine");
+        }
+        ++ctx->launches;
+    }
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Kernel launch table, one per limb count L (1..9).  Each table is compiled
+// in its own translation unit (kernels.cu with -DHMPC_L=<L>) so the builds
+// run in parallel; the C-ABI layer picks the table by the modulus' L.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "chacha.cuh"
+#include "ntt.cuh"
+
+namespace hmpc_gb300
+{
+    constexpr int max_device_limbs = 9;
+    constexpr int max_wide_words = 2 * max_device_limbs + 2;
+
+    struct HostModulus
+    {
+        int limbs = 0;
+        int bits = 0;
+        uint32_t ninv = 0;
+        uint32_t q[16] = {};
+        uint32_t one[16] = {};
+        uint32_t r2[16] = {};
+        uint32_t half[16] = {};
+    };
+
+    // constants of a centred lift from a source modulus into the target one
+    // (hmpc/ints/mod.hpp:259-307)
+    struct CastParams
+    {
+        uint32_t src_limbs;
+        uint32_t src_ninv;
+        uint32_t src_q[max_device_limbs];
+        uint32_t src_half[max_device_limbs];
+        uint32_t offset[max_device_limbs + 1];  // added when the value exceeds src/2
+        uint32_t norm_words;                      // words of value + offset
+        uint32_t direct;                          // 1: value + offset < target Q
+        uint32_t factor[max_device_limbs];        // R^2 (direct) or R'*R^2 mod Q
+    };
+
+    struct KernelTable
+    {
+        cudaError_t (*ntt_pass)(const NttPassParams& p, int kind, int nw, const HostModulus& m, unsigned grid,
+                                unsigned block, size_t smem, cudaStream_t stream);
+        cudaError_t (*fma)(uint32_t* d, const uint32_t* a, const uint32_t* b, const uint32_t* c, uint64_t elements,
+                           const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*binary)(uint32_t* out, const uint32_t* a, uint64_t a_elements, const uint32_t* b,
+                              uint64_t b_elements, uint64_t elements, int op, const HostModulus& m,
+                              cudaStream_t stream);
+        cudaError_t (*lhe_combine)(uint32_t* out, const uint32_t* k, uint64_t n, const uint32_t* u,
+                                   const uint32_t* v, const uint32_t* msg, uint64_t elements,
+                                   const uint32_t* p_mont, const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*uniform)(uint32_t* out, uint64_t elements, const RngKey& rng, int words, uint32_t top_mask,
+                               const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*cbd)(uint32_t* out, uint64_t elements, const RngKey& rng, uint32_t vx2,
+                           const uint32_t* small_table, const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*to_montgomery)(uint32_t* out, const uint32_t* in, uint64_t elements, const HostModulus& m,
+                                     cudaStream_t stream);
+        cudaError_t (*from_montgomery)(uint32_t* out, const uint32_t* in, uint64_t elements, const HostModulus& m,
+                                       cudaStream_t stream);
+        cudaError_t (*cast)(uint32_t* out, const uint32_t* in, uint64_t elements, const CastParams& cp,
+                            const HostModulus& m, cudaStream_t stream);
+        int radix_bits;
+    };
+
+    const KernelTable* kernel_table_1();
+    const KernelTable* kernel_table_2();
+    const KernelTable* kernel_table_3();
+    const KernelTable* kernel_table_4();
+    const KernelTable* kernel_table_5();
+    const KernelTable* kernel_table_6();
+    const KernelTable* kernel_table_7();
+    const KernelTable* kernel_table_8();
+    const KernelTable* kernel_table_9();
+
+    inline const KernelTable* kernel_table(int limbs)
+    {
+        switch (limbs)
+        {
+        case 1: return kernel_table_1();
+        case 2: return kernel_table_2();
+        case 3: return kernel_table_3();
+        case 4: return kernel_table_4();
+        case 5: return kernel_table_5();
+        case 6: return kernel_table_6();
+        case 7: return kernel_table_7();
+        case 8: return kernel_table_8();
+        case 9: return kernel_table_9();
+        default: return nullptr;
+        }
+    }
+}

@@ -1,0 +1,240 @@
+// Per-limb-count kernel instantiations and launchers.  Compiled once per L
+// with -DHMPC_L=<L>; exports kernel_table_<L>().
+#include <algorithm>
+
+#include "cast.cuh"
+#include "dispatch.hpp"
+#include "elementwise.cuh"
+#include "ntt.cuh"
+
+#ifndef HMPC_L
+#error "compile with -DHMPC_L=<limbs>"
+#endif
+
+#define HMPC_CAT2(a, b) a##b
+#define HMPC_CAT(a, b) HMPC_CAT2(a, b)
+
+namespace hmpc_gb300
+{
+    namespace
+    {
+        constexpr int L = HMPC_L;
+        constexpr int R = 3;  // 8 elements per thread in the NTT passes
+
+        Modulus<L> device_modulus(const HostModulus& h)
+        {
+            Modulus<L> m{};
+            for (int j = 0; j < L; ++j)
+            {
+                m.q[j] = h.q[j];
+                m.one[j] = h.one[j];
+            }
+            m.ninv = h.ninv;
+            m.bits = static_cast<uint32_t>(h.bits);
+            return m;
+        }
+
+        Modulus<L> holder(const uint32_t* words)
+        {
+            Modulus<L> m{};
+            for (int j = 0; j < L; ++j)
+            {
+                m.one[j] = words[j];
+            }
+            return m;
+        }
+
+        unsigned grid_for(uint64_t work, unsigned block)
+        {
+            const uint64_t g = (work + block - 1) / block;
+            return static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(g, 152ull * 64ull)));
+        }
+
+        template<int Kind, int NW>
+        cudaError_t launch_pass(const NttPassParams& p, const Modulus<L>& m, unsigned grid, unsigned block,
+                                size_t smem, cudaStream_t stream)
+        {
+            auto kernel = ntt_pass_kernel<L, R, Kind, NW>;
+            static bool configured = false;
+            if (!configured)
+            {
+                cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+                if (e != cudaSuccess)
+                {
+                    return e;
+                }
+                configured = true;
+            }
+            kernel<<<grid, block, smem, stream>>>(p, m);
+            return cudaGetLastError();
+        }
+
+        cudaError_t ntt_pass(const NttPassParams& p, int kind, int nw, const HostModulus& h, unsigned grid,
+                             unsigned block, size_t smem, cudaStream_t stream)
+        {
+            const Modulus<L> m = device_modulus(h);
+            if (kind == producer_tensor)
+            {
+                return launch_pass<producer_tensor, 1>(p, m, grid, block, smem, stream);
+            }
+            if (kind == producer_cbd)
+            {
+                switch (nw)
+                {
+                case 1: return launch_pass<producer_cbd, 1>(p, m, grid, block, smem, stream);
+                case 2: return launch_pass<producer_cbd, 2>(p, m, grid, block, smem, stream);
+                case 3: return launch_pass<producer_cbd, 3>(p, m, grid, block, smem, stream);
+                case 4: return launch_pass<producer_cbd, 4>(p, m, grid, block, smem, stream);
+                default: return cudaErrorInvalidValue;
+                }
+            }
+            if (kind == producer_uniform)
+            {
+                if (nw == L + 2)
+                {
+                    return launch_pass<producer_uniform, L + 2>(p, m, grid, block, smem, stream);
+                }
+                if (nw == L + 3)
+                {
+                    return launch_pass<producer_uniform, L + 3>(p, m, grid, block, smem, stream);
+                }
+            }
+            return cudaErrorInvalidValue;
+        }
+
+        cudaError_t fma(uint32_t* d, const uint32_t* a, const uint32_t* b, const uint32_t* c, uint64_t elements,
+                        const HostModulus& h, cudaStream_t stream)
+        {
+            const uintptr_t align = reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
+                                    reinterpret_cast<uintptr_t>(c) | reinterpret_cast<uintptr_t>(d);
+            const int vectorised = (elements % vec == 0) && (align % 16 == 0);
+            const unsigned block = 256;
+            unsigned grid;
+            if (vectorised)
+            {
+                grid = static_cast<unsigned>((elements / vec + block - 1) / block);
+            }
+            else
+            {
+                grid = grid_for(elements, block);
+            }
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            fma_kernel<L><<<grid, block, 0, stream>>>(d, a, b, c, elements, vectorised, device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t binary(uint32_t* out, const uint32_t* a, uint64_t a_elements, const uint32_t* b,
+                           uint64_t b_elements, uint64_t elements, int op, const HostModulus& h, cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            binary_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, a, a_elements, b, b_elements,
+                                                                          elements, op, device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t lhe_combine(uint32_t* out, const uint32_t* k, uint64_t n, const uint32_t* u, const uint32_t* v,
+                                const uint32_t* msg, uint64_t elements, const uint32_t* p_mont, const HostModulus& h,
+                                cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            lhe_combine_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, k, n, u, v, msg, elements,
+                                                                               device_modulus(h), holder(p_mont));
+            return cudaGetLastError();
+        }
+
+        cudaError_t uniform(uint32_t* out, uint64_t elements, const RngKey& rng, int words, uint32_t top_mask,
+                            const HostModulus& h, cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            const unsigned grid = grid_for(elements, 256);
+            if (words == L + 2)
+            {
+                uniform_kernel<L, L + 2><<<grid, 256, 0, stream>>>(out, elements, rng, top_mask, device_modulus(h));
+            }
+            else if (words == L + 3)
+            {
+                uniform_kernel<L, L + 3><<<grid, 256, 0, stream>>>(out, elements, rng, top_mask, device_modulus(h));
+            }
+            else
+            {
+                return cudaErrorInvalidValue;
+            }
+            return cudaGetLastError();
+        }
+
+        cudaError_t cbd(uint32_t* out, uint64_t elements, const RngKey& rng, uint32_t vx2, const uint32_t* table,
+                        const HostModulus& h, cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            const unsigned grid = grid_for(elements, 256);
+            const Modulus<L> m = device_modulus(h);
+            switch ((2 * vx2 + 31) / 32)
+            {
+            case 1: cbd_kernel<L, 1><<<grid, 256, 0, stream>>>(out, elements, rng, vx2, table, m); break;
+            case 2: cbd_kernel<L, 2><<<grid, 256, 0, stream>>>(out, elements, rng, vx2, table, m); break;
+            case 3: cbd_kernel<L, 3><<<grid, 256, 0, stream>>>(out, elements, rng, vx2, table, m); break;
+            case 4: cbd_kernel<L, 4><<<grid, 256, 0, stream>>>(out, elements, rng, vx2, table, m); break;
+            default: return cudaErrorInvalidValue;
+            }
+            return cudaGetLastError();
+        }
+
+        cudaError_t to_montgomery(uint32_t* out, const uint32_t* in, uint64_t elements, const HostModulus& h,
+                                  cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            to_montgomery_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, in, elements, holder(h.r2),
+                                                                                 device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t from_montgomery(uint32_t* out, const uint32_t* in, uint64_t elements, const HostModulus& h,
+                                    cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            from_montgomery_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, in, elements,
+                                                                                   device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t cast(uint32_t* out, const uint32_t* in, uint64_t elements, const CastParams& cp,
+                         const HostModulus& h, cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            cast_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, in, elements, cp, device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd,
+                                   to_montgomery, from_montgomery, cast, R};
+    }
+
+    const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()
+    {
+        return &table;
+    }
+}

@@ -1,0 +1,326 @@
+// Multi-limb modular arithmetic for sm_103a.
+//
+// Residues are L 32-bit limbs (least significant first) holding the fully
+// reduced Montgomery representative x*R mod Q, R = 2^(32L) -- the same
+// representation as hmpc's mod<Q> (hmpc/ints/mod.hpp:73-193), so any exact
+// implementation of the operations below reproduces the reference bit for bit.
+//
+// Carry propagation uses PTX carry chains (add.cc / addc / mad.lo.cc /
+// madc.hi.cc).  Each chain is a run of consecutive volatile asm statements; no
+// other instruction in between touches the condition code.
+#pragma once
+
+#include <cstdint>
+
+namespace hmpc_gb300
+{
+    template<int L>
+    struct Modulus
+    {
+        uint32_t q[L];
+        uint32_t one[L];    // R mod Q (Montgomery one)
+        uint32_t ninv;      // -Q^{-1} mod 2^32
+        uint32_t bits;      // bit_width(Q - 1)
+    };
+
+    namespace ptx
+    {
+        __device__ __forceinline__ uint32_t add_cc(uint32_t a, uint32_t b)
+        {
+            uint32_t r;
+            asm volatile("add.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t addc_cc(uint32_t a, uint32_t b)
+        {
+            uint32_t r;
+            asm volatile("addc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t addc(uint32_t a, uint32_t b)
+        {
+            uint32_t r;
+            asm volatile("addc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t sub_cc(uint32_t a, uint32_t b)
+        {
+            uint32_t r;
+            asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t subc_cc(uint32_t a, uint32_t b)
+        {
+            uint32_t r;
+            asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t subc(uint32_t a, uint32_t b)
+        {
+            uint32_t r;
+            asm volatile("subc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+            return r;
+        }
+        // d = lo(a*b) + c, sets carry
+        __device__ __forceinline__ uint32_t mad_lo_cc(uint32_t a, uint32_t b, uint32_t c)
+        {
+            uint32_t r;
+            asm volatile("mad.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t madc_lo_cc(uint32_t a, uint32_t b, uint32_t c)
+        {
+            uint32_t r;
+            asm volatile("madc.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t mad_hi_cc(uint32_t a, uint32_t b, uint32_t c)
+        {
+            uint32_t r;
+            asm volatile("mad.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+            return r;
+        }
+        __device__ __forceinline__ uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c)
+        {
+            uint32_t r;
+            asm volatile("madc.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+            return r;
+        }
+    }
+
+    // r = (a + b) mod Q for a, b < Q (hmpc/ints/mod.hpp:17-34).
+    template<int L>
+    __device__ __forceinline__ void mod_add(uint32_t (&r)[L], const uint32_t (&a)[L], const uint32_t (&b)[L],
+                                            const Modulus<L>& m)
+    {
+        uint32_t s[L];
+        s[0] = ptx::add_cc(a[0], b[0]);
+#pragma unroll
+        for (int j = 1; j < L; ++j)
+        {
+            s[j] = ptx::addc_cc(a[j], b[j]);
+        }
+        uint32_t top = ptx::addc(0u, 0u);
+        uint32_t d[L];
+        d[0] = ptx::sub_cc(s[0], m.q[0]);
+#pragma unroll
+        for (int j = 1; j < L; ++j)
+        {
+            d[j] = ptx::subc_cc(s[j], m.q[j]);
+        }
+        uint32_t borrow = ptx::subc(top, 0u);  // 0xffffffff when s < Q
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            r[j] = borrow ? s[j] : d[j];
+        }
+    }
+
+    // r = (a - b) mod Q for a, b < Q (hmpc/ints/mod.hpp:35-40).
+    template<int L>
+    __device__ __forceinline__ void mod_sub(uint32_t (&r)[L], const uint32_t (&a)[L], const uint32_t (&b)[L],
+                                            const Modulus<L>& m)
+    {
+        uint32_t d[L];
+        d[0] = ptx::sub_cc(a[0], b[0]);
+#pragma unroll
+        for (int j = 1; j < L; ++j)
+        {
+            d[j] = ptx::subc_cc(a[j], b[j]);
+        }
+        uint32_t mask = ptx::subc(0u, 0u);  // 0xffffffff on borrow
+        r[0] = ptx::add_cc(d[0], m.q[0] & mask);
+#pragma unroll
+        for (int j = 1; j < L - 1; ++j)
+        {
+            r[j] = ptx::addc_cc(d[j], m.q[j] & mask);
+        }
+        if (L > 1)
+        {
+            r[L - 1] = ptx::addc(d[L - 1], m.q[L - 1] & mask);
+        }
+    }
+
+    // r = -a mod Q (hmpc/ints/mod.hpp:327-341).
+    template<int L>
+    __device__ __forceinline__ void mod_neg(uint32_t (&r)[L], const uint32_t (&a)[L], const Modulus<L>& m)
+    {
+        uint32_t z[L];
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            z[j] = 0u;
+        }
+        mod_sub<L>(r, z, a, m);
+    }
+
+    // Montgomery product r = a*b*R^{-1} mod Q, a, b < Q, coarsely integrated
+    // operand scanning with one word of headroom; the result is fully reduced,
+    // which is what hmpc's schoolbook + separated REDC yields
+    // (hmpc/ints/mod.hpp:41-46, hmpc/core/num/modulo.hpp:30-66).
+    template<int L>
+    __device__ __forceinline__ void mont_mul(uint32_t (&r)[L], const uint32_t (&a)[L], const uint32_t (&b)[L],
+                                             const Modulus<L>& m)
+    {
+        uint32_t t[L + 2];
+#pragma unroll
+        for (int j = 0; j < L + 2; ++j)
+        {
+            t[j] = 0u;
+        }
+#pragma unroll
+        for (int i = 0; i < L; ++i)
+        {
+            const uint32_t bi = b[i];
+            // t += a * b_i : low halves into t[j], high halves into t[j+1]
+            t[0] = ptx::mad_lo_cc(a[0], bi, t[0]);
+#pragma unroll
+            for (int j = 1; j < L; ++j)
+            {
+                t[j] = ptx::madc_lo_cc(a[j], bi, t[j]);
+            }
+            t[L] = ptx::addc_cc(t[L], 0u);
+            t[L + 1] = ptx::addc(t[L + 1], 0u);
+            t[1] = ptx::mad_hi_cc(a[0], bi, t[1]);
+#pragma unroll
+            for (int j = 1; j < L; ++j)
+            {
+                t[j + 1] = ptx::madc_hi_cc(a[j], bi, t[j + 1]);
+            }
+            t[L + 1] = ptx::addc(t[L + 1], 0u);
+            // t += (t_0 * N') * Q, then drop the zero low word
+            const uint32_t mq = t[0] * m.ninv;
+            t[0] = ptx::mad_lo_cc(mq, m.q[0], t[0]);
+#pragma unroll
+            for (int j = 1; j < L; ++j)
+            {
+                t[j] = ptx::madc_lo_cc(mq, m.q[j], t[j]);
+            }
+            t[L] = ptx::addc_cc(t[L], 0u);
+            t[L + 1] = ptx::addc(t[L + 1], 0u);
+            t[1] = ptx::mad_hi_cc(mq, m.q[0], t[1]);
+#pragma unroll
+            for (int j = 1; j < L; ++j)
+            {
+                t[j + 1] = ptx::madc_hi_cc(mq, m.q[j], t[j + 1]);
+            }
+            t[L + 1] = ptx::addc(t[L + 1], 0u);
+#pragma unroll
+            for (int j = 0; j < L + 1; ++j)
+            {
+                t[j] = t[j + 1];
+            }
+            t[L + 1] = 0u;
+        }
+        // t < 2Q: subtract Q once if t >= Q
+        uint32_t d[L];
+        d[0] = ptx::sub_cc(t[0], m.q[0]);
+#pragma unroll
+        for (int j = 1; j < L; ++j)
+        {
+            d[j] = ptx::subc_cc(t[j], m.q[j]);
+        }
+        uint32_t borrow = ptx::subc(t[L], 0u);
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            r[j] = borrow ? t[j] : d[j];
+        }
+    }
+
+    // Reduction of a W-word value with R' = 2^(32W) (hmpc/core/num/modulo.hpp
+    // :30-66 with auxiliary power W); used by the uniform sampler
+    // (hmpc/ints/mod.hpp:210-215), where W >= L.
+    template<int L, int W>
+    __device__ __forceinline__ void redc_wide(uint32_t (&r)[L], const uint32_t (&v)[W], const Modulus<L>& m)
+    {
+        uint32_t t[W + L + 1];
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+        {
+            t[j] = v[j];
+        }
+#pragma unroll
+        for (int j = W; j < W + L + 1; ++j)
+        {
+            t[j] = 0u;
+        }
+#pragma unroll
+        for (int i = 0; i < W; ++i)
+        {
+            const uint32_t mq = t[i] * m.ninv;
+            t[i] = ptx::mad_lo_cc(mq, m.q[0], t[i]);
+#pragma unroll
+            for (int j = 1; j < L; ++j)
+            {
+                t[i + j] = ptx::madc_lo_cc(mq, m.q[j], t[i + j]);
+            }
+#pragma unroll
+            for (int k = i + L; k < W + L + 1; ++k)
+            {
+                t[k] = ptx::addc_cc(t[k], 0u);
+            }
+            t[i + 1] = ptx::mad_hi_cc(mq, m.q[0], t[i + 1]);
+#pragma unroll
+            for (int j = 1; j < L; ++j)
+            {
+                t[i + j + 1] = ptx::madc_hi_cc(mq, m.q[j], t[i + j + 1]);
+            }
+#pragma unroll
+            for (int k = i + L + 1; k < W + L + 1; ++k)
+            {
+                t[k] = ptx::addc_cc(t[k], 0u);
+            }
+        }
+        uint32_t d[L];
+        d[0] = ptx::sub_cc(t[W], m.q[0]);
+#pragma unroll
+        for (int j = 1; j < L; ++j)
+        {
+            d[j] = ptx::subc_cc(t[W + j], m.q[j]);
+        }
+        uint32_t borrow = ptx::subc(t[W + L], 0u);
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            r[j] = borrow ? t[W + j] : d[j];
+        }
+    }
+
+    template<int L>
+    __device__ __forceinline__ void set_zero(uint32_t (&r)[L])
+    {
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            r[j] = 0u;
+        }
+    }
+
+    template<int L>
+    __device__ __forceinline__ bool is_zero(const uint32_t (&a)[L])
+    {
+        uint32_t acc = 0u;
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            acc |= a[j];
+        }
+        return acc == 0u;
+    }
+
+    // a > b for L-limb unsigned integers
+    template<int L>
+    __device__ __forceinline__ bool greater(const uint32_t (&a)[L], const uint32_t (&b)[L])
+    {
+        // b - a borrows iff a > b
+        uint32_t d = ptx::sub_cc(b[0], a[0]);
+#pragma unroll
+        for (int j = 1; j < L; ++j)
+        {
+            d = ptx::subc_cc(b[j], a[j]);
+        }
+        (void)d;
+        return ptx::subc(0u, 0u) != 0u;
+    }
+}

@@ -1,0 +1,344 @@
+// Negacyclic NTT / INTT as a sequence of shared-memory tile passes.
+//
+// Semantics are those of hmpc's stage-per-kernel transform
+// (hmpc/expr/number_theoretic_transform.hpp:90-197,262-549):
+//   forward stage s: length = 2^s, step = N/2^(s+1), the lower element idx of
+//     a pair takes psi = T[2^s + (idx >> (n - s))]; v *= psi; (u+v, u-v)
+//   inverse stage s: length = N/2^(s+1), step = 2^s,
+//     psi = T[N/2^(s+1) + (idx >> (s+1))]; (u+v, (u-v)*psi); the last stage
+//     multiplies u+v by T[0] = N^-1 and u-v by T[1] (pre-multiplied by N^-1)
+// The butterflies are the same ones on the same positions, so the output
+// (natural order in -> bit-reversed order out for the forward transform) is
+// identical; only the schedule differs.
+//
+// Schedule: the log2(N) stages are split into passes.  A pass covers stages
+// [s0, s1); the element-index bits those stages touch are the "row" bits of a
+// tile.  One CTA stages T tiles (x 2^c columns for coalescing) in shared
+// memory, limb-planar.  Inside a pass, stages are processed in groups of up
+// to R: each thread holds 2^R elements in registers, applies the group's
+// butterflies there, and writes them back, so shared memory is touched once
+// per group instead of once per stage.  The first pass can generate its input
+// in registers (ChaCha20 samplers) instead of reading a tensor.
+#pragma once
+
+#include <cstdint>
+
+#include "chacha.cuh"
+#include "limbs.cuh"
+
+namespace hmpc_gb300
+{
+    enum ProducerKind : int
+    {
+        producer_tensor = 0,   // read `src` (or the output buffer when src == nullptr)
+        producer_cbd = 1,      // centred binomial, 2V = vx2, NW words per sample
+        producer_uniform = 2,  // uniform mod Q, W words per sample
+    };
+
+    constexpr int max_groups = 8;
+
+    struct NttGroup
+    {
+        uint32_t stage;          // first stage of the group
+        uint32_t count;          // stages in the group (<= R)
+        uint32_t reg_pos[6];     // local bit position of register bit k (k < R)
+        uint32_t rest_mask;      // local bits enumerated by the thread's block id
+    };
+
+    struct NttPassParams
+    {
+        uint32_t* out;                 // limb-planar, `elements` entries per limb
+        const uint32_t* src;           // tensor producer input (nullptr: read out)
+        const uint32_t* twiddles;      // element-major [N][L]
+        const uint32_t* small_table;   // Montgomery forms of 0..64, element-major
+        uint64_t elements;             // batch * N
+        uint64_t tiles;                // batch * tiles per polynomial
+        uint32_t log_n;
+        uint32_t inverse;
+        uint32_t s0, s1;               // stages of this pass
+        uint32_t row_shift;            // element bit of the lowest row bit
+        uint32_t col_bits;             // c
+        uint32_t tile_bits;            // log2 tiles per CTA
+        uint32_t local_bits;           // log2 elements per CTA = tile_bits + w + c
+        uint32_t num_groups;
+        NttGroup groups[max_groups];
+        RngKey rng;
+        uint32_t vx2;                  // 2V for the CBD producer
+        uint32_t top_mask;             // uniform producer: mask of the top word
+    };
+
+    __device__ __forceinline__ uint32_t smem_addr(uint32_t local)
+    {
+        return local + (local >> 5);  // one pad word per 32: spreads strided accesses over banks
+    }
+
+    // scatter the low bits of v into the set bits of mask (ascending)
+    __device__ __forceinline__ uint32_t deposit_bits(uint32_t v, uint32_t mask)
+    {
+        uint32_t r = 0;
+        while (mask)
+        {
+            const uint32_t low = mask & (0u - mask);
+            if (v & 1u)
+            {
+                r |= low;
+            }
+            v >>= 1;
+            mask ^= low;
+        }
+        return r;
+    }
+
+    template<int L>
+    struct NttTileGeometry
+    {
+        uint32_t w, c, tile_bits, rs, log_n;
+        uint64_t tile0;  // first global tile of this CTA
+        uint64_t n;
+
+        // element index inside its polynomial, and the polynomial, of a CTA-local index
+        __device__ __forceinline__ uint64_t tile_of(uint32_t local) const
+        {
+            return tile0 + (local >> (c + w));
+        }
+
+        __device__ __forceinline__ void locate(uint32_t local, uint64_t& poly, uint64_t& idx) const
+        {
+            const uint32_t col = local & ((1u << c) - 1u);
+            const uint32_t row = (local >> c) & ((1u << w) - 1u);
+            const uint64_t tile = tile_of(local);
+            const uint32_t tile_bits_per_poly = log_n - w - c;
+            const uint64_t t_in_poly = tile & ((1ull << tile_bits_per_poly) - 1ull);
+            poly = tile >> tile_bits_per_poly;
+            const uint64_t mid = t_in_poly & ((1ull << (rs - c)) - 1ull);
+            const uint64_t top = t_in_poly >> (rs - c);
+            idx = (top << (rs + w)) | (static_cast<uint64_t>(row) << rs) | (mid << c) | col;
+        }
+    };
+
+    template<int L, int Kind, int NW>
+    __device__ __forceinline__ void produce_pair(const NttPassParams& p, const Modulus<L>& m, uint64_t poly,
+                                                 uint64_t idx_u, uint64_t idx_v, uint32_t (&u)[L],
+                                                 uint32_t (&v)[L])
+    {
+        if constexpr (Kind == producer_cbd)
+        {
+            // one generator per pair, counter = low word of the first element's
+            // linear index; u draws first, v next (number_theoretic_transform.hpp
+            // :316-329, comp/queue.hpp:191-212)
+            uint32_t w[2 * NW];
+            chacha_stream<2 * NW>(p.rng, static_cast<uint32_t>(poly * (1ull << p.log_n) + idx_u), w);
+            int a = 0, b = 0;
+            const int count = 2 * static_cast<int>(p.vx2);
+#pragma unroll
+            for (int i = 0; i < NW; ++i)
+            {
+                uint32_t mask = 0xffffffffu;
+                if (i == NW - 1 && (count & 31))
+                {
+                    mask = (1u << (count & 31)) - 1u;
+                }
+                a += __popc(w[i] & mask);
+                b += __popc(w[NW + i] & mask);
+            }
+            small_to_mont<L>(u, a - static_cast<int>(p.vx2), p.small_table, m);
+            small_to_mont<L>(v, b - static_cast<int>(p.vx2), p.small_table, m);
+        }
+        else if constexpr (Kind == producer_uniform)
+        {
+            uint32_t w[2 * NW];
+            chacha_stream<2 * NW>(p.rng, static_cast<uint32_t>(poly * (1ull << p.log_n) + idx_u), w);
+            uniform_from_words<L, NW, 0, 2 * NW>(u, w, p.top_mask, m);
+            uniform_from_words<L, NW, NW, 2 * NW>(v, w, p.top_mask, m);
+        }
+        else
+        {
+            (void)idx_v;
+        }
+    }
+
+    template<int L>
+    __device__ __forceinline__ void load_twiddle(uint32_t (&t)[L], const uint32_t* table, uint64_t index)
+    {
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            t[j] = __ldg(table + index * L + j);
+        }
+    }
+
+    // One pass over the tiles of a batch.  R = register bits per thread.
+    template<int L, int R, int Kind, int NW>
+    __global__ void __launch_bounds__(256) ntt_pass_kernel(const NttPassParams p, const Modulus<L> m)
+    {
+        extern __shared__ uint32_t smem[];
+        constexpr int regs = 1 << R;
+        const uint32_t local_count = 1u << p.local_bits;
+        const uint32_t limb_stride = smem_addr(local_count);
+        const uint32_t w = p.s1 - p.s0;
+
+        NttTileGeometry<L> geo;
+        geo.w = w;
+        geo.c = p.col_bits;
+        geo.tile_bits = p.tile_bits;
+        geo.rs = p.row_shift;
+        geo.log_n = p.log_n;
+        geo.n = 1ull << p.log_n;
+        geo.tile0 = static_cast<uint64_t>(blockIdx.x) << p.tile_bits;
+
+        const bool fused = Kind != producer_tensor;
+        if (!fused)
+        {
+            const uint32_t* in = p.src ? p.src : p.out;
+            for (uint32_t local = threadIdx.x; local < local_count; local += blockDim.x)
+            {
+                if (geo.tile_of(local) >= p.tiles)
+                {
+                    continue;  // partial last CTA: nothing to load, nothing is stored
+                }
+                uint64_t poly, idx;
+                geo.locate(local, poly, idx);
+                const uint64_t e = poly * geo.n + idx;
+#pragma unroll
+                for (int j = 0; j < L; ++j)
+                {
+                    smem[j * limb_stride + smem_addr(local)] = in[static_cast<uint64_t>(j) * p.elements + e];
+                }
+            }
+            __syncthreads();
+        }
+
+        for (uint32_t gi = 0; gi < p.num_groups; ++gi)
+        {
+            const NttGroup& g = p.groups[gi];
+            uint32_t off[regs];
+#pragma unroll
+            for (int x = 0; x < regs; ++x)
+            {
+                uint32_t o = 0;
+#pragma unroll
+                for (int k = 0; k < R; ++k)
+                {
+                    if (x & (1 << k))
+                    {
+                        o |= 1u << g.reg_pos[k];
+                    }
+                }
+                off[x] = o;
+            }
+            const uint32_t blocks = local_count >> R;
+            for (uint32_t b = threadIdx.x; b < blocks; b += blockDim.x)
+            {
+                const uint32_t base = deposit_bits(b, g.rest_mask);
+                uint32_t x_reg[regs][L];
+                if (fused && gi == 0)
+                {
+                    // stage 0 pairs register bit 0: (x, x | 1)
+#pragma unroll
+                    for (int x = 0; x < regs; x += 2)
+                    {
+                        uint64_t poly, idx_u, idx_v;
+                        geo.locate(base | off[x], poly, idx_u);
+                        geo.locate(base | off[x | 1], poly, idx_v);
+                        produce_pair<L, Kind, NW>(p, m, poly, idx_u, idx_v, x_reg[x], x_reg[x | 1]);
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int x = 0; x < regs; ++x)
+                    {
+                        const uint32_t a = smem_addr(base | off[x]);
+#pragma unroll
+                        for (int j = 0; j < L; ++j)
+                        {
+                            x_reg[x][j] = smem[j * limb_stride + a];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < R; ++k)
+                {
+                    if (static_cast<uint32_t>(k) < g.count)
+                    {
+                        const uint32_t s = g.stage + k;
+                        const bool last_inverse = p.inverse && s == p.log_n - 1;
+#pragma unroll
+                        for (int x = 0; x < regs; ++x)
+                        {
+                            if ((x & (1 << k)) == 0)
+                            {
+                                uint64_t poly, idx;
+                                geo.locate(base | off[x], poly, idx);
+                                uint32_t t[L];
+                                if (!p.inverse)
+                                {
+                                    load_twiddle<L>(t, p.twiddles, (1ull << s) + (idx >> (p.log_n - s)));
+                                    mont_mul<L>(x_reg[x | (1 << k)], x_reg[x | (1 << k)], t, m);
+                                    uint32_t sum[L];
+                                    mod_add<L>(sum, x_reg[x], x_reg[x | (1 << k)], m);
+                                    mod_sub<L>(x_reg[x | (1 << k)], x_reg[x], x_reg[x | (1 << k)], m);
+#pragma unroll
+                                    for (int j = 0; j < L; ++j)
+                                    {
+                                        x_reg[x][j] = sum[j];
+                                    }
+                                }
+                                else if (!last_inverse)
+                                {
+                                    load_twiddle<L>(t, p.twiddles, (geo.n >> (s + 1)) + (idx >> (s + 1)));
+                                    uint32_t sum[L], diff[L];
+                                    mod_add<L>(sum, x_reg[x], x_reg[x | (1 << k)], m);
+                                    mod_sub<L>(diff, x_reg[x], x_reg[x | (1 << k)], m);
+                                    mont_mul<L>(x_reg[x | (1 << k)], diff, t, m);
+#pragma unroll
+                                    for (int j = 0; j < L; ++j)
+                                    {
+                                        x_reg[x][j] = sum[j];
+                                    }
+                                }
+                                else
+                                {
+                                    uint32_t sum[L], diff[L];
+                                    mod_add<L>(sum, x_reg[x], x_reg[x | (1 << k)], m);
+                                    mod_sub<L>(diff, x_reg[x], x_reg[x | (1 << k)], m);
+                                    load_twiddle<L>(t, p.twiddles, 0);
+                                    mont_mul<L>(x_reg[x], sum, t, m);
+                                    load_twiddle<L>(t, p.twiddles, 1);
+                                    mont_mul<L>(x_reg[x | (1 << k)], diff, t, m);
+                                }
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int x = 0; x < regs; ++x)
+                {
+                    const uint32_t a = smem_addr(base | off[x]);
+#pragma unroll
+                    for (int j = 0; j < L; ++j)
+                    {
+                        smem[j * limb_stride + a] = x_reg[x][j];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
+        for (uint32_t local = threadIdx.x; local < local_count; local += blockDim.x)
+        {
+            if (geo.tile_of(local) >= p.tiles)
+            {
+                continue;
+            }
+            uint64_t poly, idx;
+            geo.locate(local, poly, idx);
+            const uint64_t e = poly * geo.n + idx;
+#pragma unroll
+            for (int j = 0; j < L; ++j)
+            {
+                p.out[static_cast<uint64_t>(j) * p.elements + e] = smem[j * limb_stride + smem_addr(local)];
+            }
+        }
+    }
+}

@@ -1,0 +1,182 @@
+/*
+ * hmpc_gb300.h -- C ABI of the GB300 (sm_103a) implementation of hmpc's
+ * data-parallel hot path: multi-limb Montgomery arithmetic, the negacyclic
+ * NTT/INTT, the elementwise modular FMA, the ChaCha20 samplers and linear BGV.
+ *
+ * This is the device boundary that hmpc's SYCL device path crosses inside
+ * hmpc::comp::queue (hmpc/comp/queue.hpp:313-414): where the reference submits
+ * a parallel_for per expression node, a host front end calls these entry
+ * points instead.  Conventions shared with the reference:
+ *
+ *  - A residue mod Q is L = ceil(bit_width(Q-1)/32) 32-bit limbs, least
+ *    significant first, holding the fully reduced Montgomery representative
+ *    x*R mod Q, R = 2^(32L) (hmpc/ints/mod.hpp:73-193).
+ *  - Tensors are caller-owned device buffers in the reference's limb-planar
+ *    layout: limb j of element e at [j*elements + e]
+ *    (hmpc/comp/tensor.hpp:21,25-29; hmpc/comp/accessor.hpp:191-197).  A batch
+ *    of polynomials of degree N stores element e = i*N + k.
+ *  - The RNG capability is the queue's: an 8-word ChaCha20 key and a 96-bit
+ *    nonce; a sampler launch uses the current nonce and then advances it by
+ *    its element count (hmpc/comp/queue.hpp:175-253).  Element e's generator
+ *    is ChaCha20(key, nonce, counter = low 32 bits of e).
+ *
+ * Every entry point returns HMPC_OK (0) or an error code and never throws;
+ * hmpc_last_error() describes the last failure of the calling thread.  Work is
+ * asynchronous on the context's stream; hmpc_context_synchronize() waits
+ * (the reference's queue.wait(), hmpc/comp/queue.hpp:531-534).
+ */
+#ifndef HMPC_GB300_H
+#define HMPC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HMPC_OK 0
+#define HMPC_ERROR_INVALID_ARGUMENT 1
+#define HMPC_ERROR_UNSUPPORTED 2
+#define HMPC_ERROR_CUDA 3
+#define HMPC_ERROR_OUT_OF_MEMORY 4
+#define HMPC_ERROR_NO_ROOT 5
+#define HMPC_ERROR_TIMEOUT 6
+#define HMPC_ERROR_REJECTED 7
+
+typedef struct hmpc_context hmpc_context;
+typedef struct hmpc_modulus hmpc_modulus;
+
+/* Description of the calling thread's last failure ("" when none). */
+const char* hmpc_last_error(void);
+/* Library version; returns HMPC_OK. */
+int hmpc_version(int* major, int* minor);
+
+/* --- context: device, stream and RNG capability -------------------------
+ * Replaces hmpc::comp::queue's constructors (hmpc/comp/queue.hpp:229-239):
+ * `key` is the 8-word ChaCha20 key (the reference draws it from
+ * std::random_device when none is given); the nonce starts at 0.  `stream` is
+ * a cudaStream_t (NULL: the legacy default stream). */
+int hmpc_context_create(int device, const uint32_t key[8], void* stream, hmpc_context** out);
+int hmpc_context_destroy(hmpc_context* ctx);
+int hmpc_context_set_stream(hmpc_context* ctx, void* stream);
+int hmpc_context_get_nonce(const hmpc_context* ctx, uint32_t nonce[3]);
+int hmpc_context_set_nonce(hmpc_context* ctx, const uint32_t nonce[3]);
+/* Number of kernels launched through this context so far (no counterpart in
+ * the reference; used to report launches per timed step). */
+int hmpc_context_launch_count(const hmpc_context* ctx, uint64_t* count);
+/* Measured 32-bit integer multiply throughput of the context's device in
+ * operations per second (mad.lo and mad.hi each count one): the denominator of
+ * the integer-pipe roofline.  No counterpart in the reference. */
+int hmpc_probe_int_multiply_rate(hmpc_context* ctx, double* ops_per_second);
+/* hmpc::comp::queue::wait (hmpc/comp/queue.hpp:531-534) */
+int hmpc_context_synchronize(hmpc_context* ctx);
+
+/* --- moduli ---------------------------------------------------------------
+ * mod<Q>'s compile-time constants (hmpc/ints/mod.hpp:90-127), computed at
+ * run time: Q is given as q_words little-endian 32-bit words.  Supported:
+ * odd Q with 2 <= bit_width(Q-1) <= 288 (1..9 limbs). */
+int hmpc_modulus_create(hmpc_context* ctx, const uint32_t* q, int q_words, hmpc_modulus** out);
+int hmpc_modulus_destroy(hmpc_modulus* mod);
+/* limbs (L), bit_width(Q-1), and R mod Q (Montgomery one, L words, may be NULL) */
+int hmpc_modulus_info(const hmpc_modulus* mod, int* limbs, int* bits, uint32_t* one);
+/* Build (once) and cache on the device the forward and inverse twiddle tables
+ * for ring degree n (hmpc/expr/number_theoretic_transform.hpp:35-88, the
+ * reference caches them per (type, N) in the queue: comp/queue.hpp:364-381).
+ * The transforms call this themselves; calling it ahead keeps the host work
+ * out of a timed or captured region. */
+int hmpc_modulus_prepare(hmpc_modulus* mod, uint64_t n);
+/* psi (inverse = 0) or psi^-1 (inverse = 1) for degree n, Montgomery form,
+ * L words (hmpc/ints/num/theory/root_of_unity.hpp:20-54). */
+int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root);
+/* Copy a cached twiddle table (n*L words, element-major) to host memory. */
+int hmpc_modulus_twiddles(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* host_table);
+
+/* --- device memory helpers (optional: any device allocation works) ------ */
+int hmpc_tensor_alloc(hmpc_context* ctx, uint64_t words, uint32_t** out);
+int hmpc_tensor_free(hmpc_context* ctx, uint32_t* ptr);
+int hmpc_tensor_upload(hmpc_context* ctx, uint32_t* dst, const uint32_t* host, uint64_t words);
+int hmpc_tensor_download(hmpc_context* ctx, uint32_t* host, const uint32_t* src, uint64_t words);
+
+/* --- transforms -------------------------------------------------------------
+ * What feeds stage 0 of a forward transform.  The reference fuses the inner
+ * expression of number_theoretic_transform(...) into its first kernel
+ * (hmpc/expr/number_theoretic_transform.hpp:262-335): a tensor, a centred
+ * binomial sampler (expr/random/binomial.hpp:176-236) or a uniform sampler
+ * (expr/random/uniform.hpp:10-58).  For a sampler both inputs of a stage-0
+ * butterfly come from one generator (counter = element index of the first),
+ * drawn one after the other, and the launch advances the nonce by batch*n. */
+#define HMPC_PRODUCER_TENSOR 0
+#define HMPC_PRODUCER_CBD 1
+#define HMPC_PRODUCER_UNIFORM 2
+typedef struct hmpc_producer
+{
+    int kind;
+    const uint32_t* src;    /* HMPC_PRODUCER_TENSOR: batch*n elements, limb-planar */
+    uint32_t variance_x2;   /* HMPC_PRODUCER_CBD: 2V (1 for V = 1/2, 20 for V = 10), 1..64 */
+    uint32_t security;      /* HMPC_PRODUCER_UNIFORM: statistical security, 80 */
+} hmpc_producer;
+
+/* number_theoretic_transform_expression (number_theoretic_transform.hpp:226-394):
+ * batch polynomials of degree n (power of two, n >= 4) in natural order ->
+ * bit-reversed order.  out may equal producer->src. */
+int hmpc_ntt_forward(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const hmpc_producer* producer,
+                     uint32_t* out);
+/* inverse_number_theoretic_transform_expression (:396-550). out may equal in. */
+int hmpc_ntt_inverse(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const uint32_t* in,
+                     uint32_t* out);
+
+/* --- elementwise ----------------------------------------------------------- */
+/* d = a*b + c (examples/fma.cpp:56-67) */
+int hmpc_fma(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* a, const uint32_t* b,
+             const uint32_t* c, uint32_t* d);
+#define HMPC_OP_ADD 0
+#define HMPC_OP_SUB 1
+#define HMPC_OP_MUL 2
+/* out[e] = a[e % a_elements] OP b[e % b_elements]: the binary expressions of
+ * hmpc/expr/binary_expression.hpp:149-163 with broadcasting of an unsqueezed
+ * operand (hmpc/expr/unsqueeze.hpp:9-61).  a_elements and b_elements must
+ * divide elements. */
+int hmpc_binary(hmpc_context* ctx, hmpc_modulus* mod, int op, uint64_t elements, const uint32_t* a,
+                uint64_t a_elements, const uint32_t* b, uint64_t b_elements, uint32_t* out);
+/* uniform<mod<Q>>(shape) evaluated elementwise (expr/random/uniform.hpp:11-46);
+ * advances the nonce by elements. security must be 80. */
+int hmpc_sample_uniform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, uint32_t security, uint32_t* out);
+/* centered_binomial<mod<Q>>(shape, V) (expr/random/binomial.hpp:176-236), 2V = variance_x2 */
+int hmpc_sample_cbd(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, uint32_t variance_x2, uint32_t* out);
+/* cast<mod<dst>>(x) of residues mod src: the centred lift of
+ * hmpc/ints/mod.hpp:259-307 (expr/cast.hpp:10-53). */
+int hmpc_cast(hmpc_context* ctx, hmpc_modulus* dst, hmpc_modulus* src, uint64_t elements, const uint32_t* in,
+              uint32_t* out);
+/* canonical integers in [0, Q) <-> Montgomery representatives
+ * (mod.hpp:197-204 and :356-361) */
+int hmpc_to_montgomery(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* in, uint32_t* out);
+int hmpc_from_montgomery(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* in, uint32_t* out);
+
+/* --- linear BGV (hmpc/expr/crypto/lhe) ---------------------------------------
+ * Keys and ciphertext components are polynomials of degree n mod q in NTT
+ * representation; plaintexts are mod p (coefficient representation, or NTT
+ * when plaintext_ntt != 0). */
+/* enc (expr/crypto/lhe/enc.hpp:19-69) with randomness<Rq>(shape{batch})
+ * (randomness.hpp:196-226): c0 = a*u + v*p + NTT_q(lift(m)), c1 = b*u + w*p
+ * with u = NTT(CBD(1/2)), v, w = NTT(CBD(10)).  Nonce order of the reference's
+ * execution plan: u, v, w each advance the nonce by batch*n. */
+int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
+                 const uint32_t* key_a, const uint32_t* key_b, const uint32_t* plaintext, int plaintext_ntt,
+                 uint32_t* c0, uint32_t* c1);
+/* dec<Plaintext>(s, ct) (expr/crypto/lhe/dec.hpp:13-45): c0 - s*c1 -> INTT_q
+ * -> cast to p (-> NTT_p when plaintext_ntt). */
+int hmpc_lhe_dec(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
+                 const uint32_t* s, const uint32_t* c0, const uint32_t* c1, int plaintext_ntt, uint32_t* out);
+/* Key generation; no counterpart in the reference, whose keys are plain
+ * tensors (comp/crypto/lhe/key.hpp:7-12).  b <- uniform mod q (NTT form),
+ * s <- NTT(CBD(1/2)), e <- NTT(CBD(10)), a = b*s + p*e, so that
+ * dec(s, enc((a, b), m)) = m.  Nonce order: b, s, e (n each). */
+int hmpc_lhe_keygen(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint32_t* s, uint32_t* a,
+                    uint32_t* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -14,6 +14,14 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: a CPU test that takes more than a few seconds")
 
 
+def pytest_sessionstart(session):
+    # the product library is built before collection so that tests import a
+    # complete extension (a missing build is an error, not a skip)
+    import hmpc_gb300
+
+    hmpc_gb300.build()
+
+
 @pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as orc
