@@ -14,12 +14,13 @@
 
 #include "dispatch.hpp"
 #include "host_math.hpp"
+#include "internal.hpp"
 #include "plan.hpp"
 #include "probe.hpp"
 
 using namespace hmpc_gb300;
 
-namespace
+namespace hmpc_gb300::detail
 {
     thread_local std::string last_error;
 
@@ -34,21 +35,6 @@ namespace
         return fail(HMPC_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     }
 
-#define HMPC_CUDA(call, what)                                                                                         \
-    do                                                                                                                \
-    {                                                                                                                 \
-        cudaError_t hmpc_e_ = (call);                                                                                 \
-        if (hmpc_e_ != cudaSuccess)                                                                                   \
-        {                                                                                                             \
-            return cuda_fail(hmpc_e_, what);                                                                          \
-        }                                                                                                             \
-    } while (0)
-
-    host::words to_words(const uint32_t* p, int n)
-    {
-        return host::words(p, p + n);
-    }
-
     void nonce_add(uint32_t nonce[3], uint64_t v)
     {
         uint64_t s = static_cast<uint64_t>(nonce[0]) + static_cast<uint32_t>(v);
@@ -57,108 +43,19 @@ namespace
         nonce[1] = static_cast<uint32_t>(s);
         nonce[2] += static_cast<uint32_t>(s >> 32);
     }
-
-    struct Tables
-    {
-        uint32_t* forward = nullptr;
-        uint32_t* inverse = nullptr;
-        host::words root, inverse_root;
-    };
 }
 
-struct hmpc_context
-{
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    uint32_t key[8] = {};
-    uint32_t nonce[3] = {};
-    uint32_t* workspace = nullptr;
-    uint64_t workspace_words = 0;
-    uint64_t launches = 0;  // kernels launched through this context
-    std::vector<hmpc_modulus*> moduli;
-
-    uint32_t* scratch(uint64_t words)
-    {
-        if (words > workspace_words)
-        {
-            if (workspace)
-            {
-                cudaStreamSynchronize(stream);
-                cudaFree(workspace);
-                workspace = nullptr;
-                workspace_words = 0;
-            }
-            if (cudaMalloc(&workspace, words * sizeof(uint32_t)) != cudaSuccess)
-            {
-                return nullptr;
-            }
-            workspace_words = words;
-        }
-        return workspace;
-    }
-
-    RngKey rng() const
-    {
-        RngKey k{};
-        std::memcpy(k.key, key, sizeof key);
-        std::memcpy(k.nonce, nonce, sizeof nonce);
-        return k;
-    }
-};
-
-struct hmpc_modulus
-{
-    hmpc_context* ctx = nullptr;
-    host::ModulusConstants c;
-    HostModulus h;
-    const KernelTable* kt = nullptr;
-    uint32_t* small_table = nullptr;  // Montgomery forms of 0..64, element-major
-    std::map<uint64_t, Tables> tables;
-
-    ~hmpc_modulus()
-    {
-        cudaFree(small_table);
-        for (auto& kv : tables)
-        {
-            cudaFree(kv.second.forward);
-            cudaFree(kv.second.inverse);
-        }
-    }
-
-    int prepare(uint64_t n, Tables** out)
-    {
-        auto it = tables.find(n);
-        if (it == tables.end())
-        {
-            Tables t;
-            std::vector<uint32_t> fwd, inv;
-            std::string error;
-            if (!host::twiddle_table(c, n, false, fwd, t.root, error) ||
-                !host::twiddle_table(c, n, true, inv, t.inverse_root, error))
-            {
-                return fail(HMPC_ERROR_NO_ROOT, error);
-            }
-            const size_t bytes = fwd.size() * sizeof(uint32_t);
-            HMPC_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-            HMPC_CUDA(cudaMalloc(&t.forward, bytes), "allocating twiddles");
-            if (cudaMalloc(&t.inverse, bytes) != cudaSuccess)
-            {
-                cudaFree(t.forward);
-                return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating twiddles");
-            }
-            HMPC_CUDA(cudaMemcpy(t.forward, fwd.data(), bytes, cudaMemcpyHostToDevice), "uploading twiddles");
-            HMPC_CUDA(cudaMemcpy(t.inverse, inv.data(), bytes, cudaMemcpyHostToDevice), "uploading twiddles");
-            it = tables.emplace(n, t).first;
-        }
-        if (out)
-        {
-            *out = &it->second;
-        }
-        return HMPC_OK;
-    }
-};
+using namespace hmpc_gb300::detail;
 
 namespace
+{
+    host::words to_words(const uint32_t* p, int n)
+    {
+        return host::words(p, p + n);
+    }
+}
+
+namespace hmpc_gb300::detail
 {
     int check_degree(uint64_t n)
     {

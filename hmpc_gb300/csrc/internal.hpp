@@ -1,0 +1,140 @@
+// Internal declarations shared by the C-ABI translation units: the opaque
+// context and modulus objects and the helpers that launch transforms.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hmpc_gb300.h"
+#include "dispatch.hpp"
+#include "host_math.hpp"
+
+namespace hmpc_gb300::detail
+{
+    int fail(int code, const std::string& message);
+    int cuda_fail(cudaError_t e, const char* what);
+    void nonce_add(uint32_t nonce[3], uint64_t v);
+
+    struct Tables
+    {
+        uint32_t* forward = nullptr;
+        uint32_t* inverse = nullptr;
+        host::words root, inverse_root;
+    };
+}
+
+#define HMPC_CUDA(call, what)                                                                                         \
+    do                                                                                                                \
+    {                                                                                                                 \
+        cudaError_t hmpc_e_ = (call);                                                                                 \
+        if (hmpc_e_ != cudaSuccess)                                                                                   \
+        {                                                                                                             \
+            return ::hmpc_gb300::detail::cuda_fail(hmpc_e_, what);                                                    \
+        }                                                                                                             \
+    } while (0)
+
+struct hmpc_context
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t key[8] = {};
+    uint32_t nonce[3] = {};
+    uint32_t* workspace = nullptr;
+    uint64_t workspace_words = 0;
+    uint64_t launches = 0;  // kernels launched through this context
+    std::vector<hmpc_modulus*> moduli;
+
+    uint32_t* scratch(uint64_t words)
+    {
+        if (words > workspace_words)
+        {
+            if (workspace)
+            {
+                cudaStreamSynchronize(stream);
+                cudaFree(workspace);
+                workspace = nullptr;
+                workspace_words = 0;
+            }
+            if (cudaMalloc(&workspace, words * sizeof(uint32_t)) != cudaSuccess)
+            {
+                return nullptr;
+            }
+            workspace_words = words;
+        }
+        return workspace;
+    }
+
+    hmpc_gb300::RngKey rng() const
+    {
+        hmpc_gb300::RngKey k{};
+        std::memcpy(k.key, key, sizeof key);
+        std::memcpy(k.nonce, nonce, sizeof nonce);
+        return k;
+    }
+};
+
+struct hmpc_modulus
+{
+    hmpc_context* ctx = nullptr;
+    hmpc_gb300::host::ModulusConstants c;
+    hmpc_gb300::HostModulus h;
+    const hmpc_gb300::KernelTable* kt = nullptr;
+    uint32_t* small_table = nullptr;  // Montgomery forms of 0..64, element-major
+    std::map<uint64_t, hmpc_gb300::detail::Tables> tables;
+
+    ~hmpc_modulus()
+    {
+        cudaFree(small_table);
+        for (auto& kv : tables)
+        {
+            cudaFree(kv.second.forward);
+            cudaFree(kv.second.inverse);
+        }
+    }
+
+    int prepare(uint64_t n, hmpc_gb300::detail::Tables** out)
+    {
+        auto it = tables.find(n);
+        if (it == tables.end())
+        {
+            hmpc_gb300::detail::Tables t;
+            std::vector<uint32_t> fwd, inv;
+            std::string error;
+            if (!hmpc_gb300::host::twiddle_table(c, n, false, fwd, t.root, error) ||
+                !hmpc_gb300::host::twiddle_table(c, n, true, inv, t.inverse_root, error))
+            {
+                return hmpc_gb300::detail::fail(HMPC_ERROR_NO_ROOT, error);
+            }
+            const size_t bytes = fwd.size() * sizeof(uint32_t);
+            HMPC_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+            HMPC_CUDA(cudaMalloc(&t.forward, bytes), "allocating twiddles");
+            if (cudaMalloc(&t.inverse, bytes) != cudaSuccess)
+            {
+                cudaFree(t.forward);
+                return hmpc_gb300::detail::fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating twiddles");
+            }
+            HMPC_CUDA(cudaMemcpy(t.forward, fwd.data(), bytes, cudaMemcpyHostToDevice), "uploading twiddles");
+            HMPC_CUDA(cudaMemcpy(t.inverse, inv.data(), bytes, cudaMemcpyHostToDevice), "uploading twiddles");
+            it = tables.emplace(n, t).first;
+        }
+        if (out)
+        {
+            *out = &it->second;
+        }
+        return HMPC_OK;
+    }
+};
+
+namespace hmpc_gb300::detail
+{
+    int check_degree(uint64_t n);
+    int enter(hmpc_context* ctx);
+    int run_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
+                      uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
+    CastParams make_cast(const hmpc_modulus* dst, const hmpc_modulus* src);
+}
