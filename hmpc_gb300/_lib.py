@@ -76,6 +76,7 @@ SIGNATURES = {
     "hmpc_to_montgomery": ([_vp, _vp, _u64, _vp, _vp], _int),
     "hmpc_from_montgomery": ([_vp, _vp, _u64, _vp, _vp], _int),
     "hmpc_lhe_enc": ([_vp, _vp, _vp, _u64, _u64, _vp, _vp, _vp, _int, _vp, _vp], _int),
+    "hmpc_lhe_enc_noalloc": ([_vp, _vp, _vp, _u64, _u64, _vp, _vp, _vp, _int, _vp, _vp], _int),
     "hmpc_lhe_dec": ([_vp, _vp, _vp, _u64, _u64, _vp, _vp, _vp, _int, _vp], _int),
     "hmpc_lhe_keygen": ([_vp, _vp, _vp, _u64, _vp, _vp, _vp], _int),
 }

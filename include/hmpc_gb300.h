@@ -164,6 +164,24 @@ int hmpc_from_montgomery(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements
 int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
                  const uint32_t* key_a, const uint32_t* key_b, const uint32_t* plaintext, int plaintext_ntt,
                  uint32_t* c0, uint32_t* c1);
+/* hmpc_lhe_enc without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory: a serving
+ * process whose memory is reserved up front by its own pool, or a
+ * latency-critical loop that must not pay the device-wide synchronisation that
+ * cudaMalloc/cudaFree can cause.  Same arguments and bit-identical results as
+ * hmpc_lhe_enc; the intermediates live in one fixed 32 MiB array of device
+ * memory in this library (held by every GPU that loads it until exit), so
+ * 3*batch*n*L_q (+ batch*n*L_p for NTT-form plaintexts) must not exceed
+ * 8 Mi words -- larger batches are rejected with HMPC_ERROR_INVALID_ARGUMENT.
+ * The twiddle tables must already exist (hmpc_modulus_prepare) -- the call
+ * refuses to build them.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls on a device share the array: calls that overlap
+ * on the GPU (other streams, other contexts) race and must be serialised by
+ * the caller. */
+int hmpc_lhe_enc_noalloc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
+                         const uint32_t* key_a, const uint32_t* key_b, const uint32_t* plaintext, int plaintext_ntt,
+                         uint32_t* c0, uint32_t* c1);
 /* dec<Plaintext>(s, ct) (expr/crypto/lhe/dec.hpp:13-45): c0 - s*c1 -> INTT_q
  * -> cast to p (-> NTT_p when plaintext_ntt). */
 int hmpc_lhe_dec(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
