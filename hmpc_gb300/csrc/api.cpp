@@ -133,6 +133,11 @@ namespace hmpc_gb300::detail
             return fail(HMPC_ERROR_INVALID_ARGUMENT, "tensor producer without source");
         }
         const int log_n = __builtin_ctzll(n);
+        if (log_n < mod->kt->radix_bits)
+        {
+            // fewer stages than one register group holds: the per-stage kernel
+            return run_plain(ctx, mod, n, batch, inverse, kind, vx2, security, src, out);
+        }
         const std::vector<PassPlan> plan = plan_transform(L, log_n, batch, inverse, mod->kt->radix_bits);
         const RngKey rng = ctx->rng();
         for (size_t i = 0; i < plan.size(); ++i)
@@ -208,6 +213,140 @@ namespace hmpc_gb300::detail
             cp.offset[j] = offset[static_cast<size_t>(j)];
         }
         return cp;
+    }
+}
+
+namespace hmpc_gb300::detail
+{
+    // x = c0 - s*c1 (+ s^2*c2) -> INTT_q -> cast to p (-> NTT_p)
+    int decrypt(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch, const uint32_t* s,
+                const uint32_t* c0, const uint32_t* c1, const uint32_t* c2, int plaintext_ntt, uint32_t* out)
+    {
+        if (int rc = enter(ctx))
+        {
+            return rc;
+        }
+        if (!q || !p || !s || !c0 || !c1 || !out)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+        }
+        if (int rc = check_degree(n))
+        {
+            return rc;
+        }
+        if (batch == 0)
+        {
+            return HMPC_OK;
+        }
+        const uint64_t elements = n * batch;
+        uint32_t* x = ctx->scratch(elements * static_cast<uint64_t>(q->c.limbs));
+        if (!x)
+        {
+            return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating the decryption workspace");
+        }
+        cudaError_t e = q->kt->dec_combine(x, s, n, c0, c1, c2, elements, q->h, ctx->stream);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "launching decryption combine");
+        }
+        ++ctx->launches;
+        int rc = run_transform(ctx, q, n, batch, true, producer_tensor, 0, 0, x, x);
+        if (rc)
+        {
+            return rc;
+        }
+        e = p->kt->cast(out, x, elements, make_cast(p, q), p->h, ctx->stream);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "launching cast");
+        }
+        ++ctx->launches;
+        if (plaintext_ntt)
+        {
+            rc = run_transform(ctx, p, n, batch, false, producer_tensor, 0, 0, out, out);
+        }
+        return rc;
+    }
+
+    // one launch per stage over global memory (plain.cuh)
+    int run_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
+                  uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out)
+    {
+        if (int rc = enter(ctx))
+        {
+            return rc;
+        }
+        if (!mod || !out)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus or output");
+        }
+        if (int rc = check_degree(n))
+        {
+            return rc;
+        }
+        if (batch == 0)
+        {
+            return HMPC_OK;
+        }
+        Tables* t = nullptr;
+        if (int rc = mod->prepare(n, &t))
+        {
+            return rc;
+        }
+        const int L = mod->c.limbs;
+        int nw = 1;
+        uint32_t top_mask = 0xffffffffu;
+        if (kind == producer_cbd)
+        {
+            if (vx2 < 1 || vx2 > 64)
+            {
+                return fail(HMPC_ERROR_UNSUPPORTED, "centred binomial needs 1 <= 2V <= 64");
+            }
+            nw = static_cast<int>((2 * vx2 + 31) / 32);
+        }
+        else if (kind == producer_uniform)
+        {
+            const uint32_t bits = static_cast<uint32_t>(mod->c.bits) + security;
+            nw = static_cast<int>((bits + 31) / 32);
+            if (nw != L + 2 && nw != L + 3)
+            {
+                return fail(HMPC_ERROR_UNSUPPORTED, "uniform sampler supports statistical security 80");
+            }
+            if (bits % 32)
+            {
+                top_mask = (1u << (bits % 32)) - 1u;
+            }
+        }
+        else if (kind != producer_tensor || !src)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "bad producer");
+        }
+        PlainStageParams p{};
+        p.out = out;
+        p.src = src;
+        p.twiddles = inverse ? t->inverse : t->forward;
+        p.small_table = mod->small_table;
+        p.elements = n * batch;
+        p.log_n = static_cast<uint32_t>(__builtin_ctzll(n));
+        p.inverse = inverse ? 1u : 0u;
+        p.rng = ctx->rng();
+        p.vx2 = vx2;
+        p.top_mask = top_mask;
+        for (uint32_t stage = 0; stage < p.log_n; ++stage)
+        {
+            p.stage = stage;
+            cudaError_t e = mod->kt->plain_stage(p, kind, nw, mod->h, ctx->stream);
+            if (e != cudaSuccess)
+            {
+                return cuda_fail(e, "launching plain stage");
+            }
+            ++ctx->launches;
+        }
+        if (kind != producer_tensor)
+        {
+            nonce_add(ctx->nonce, n * batch);
+        }
+        return HMPC_OK;
     }
 }
 
@@ -757,54 +896,55 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
 int hmpc_lhe_dec(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
                  const uint32_t* s, const uint32_t* c0, const uint32_t* c1, int plaintext_ntt, uint32_t* out)
 {
+    return decrypt(ctx, q, p, n, batch, s, c0, c1, nullptr, plaintext_ntt, out);
+}
+
+int hmpc_lhe_dec2(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
+                  const uint32_t* s, const uint32_t* c0, const uint32_t* c1, const uint32_t* c2, int plaintext_ntt,
+                  uint32_t* out)
+{
+    if (!c2)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null c2");
+    }
+    return decrypt(ctx, q, p, n, batch, s, c0, c1, c2, plaintext_ntt, out);
+}
+
+int hmpc_lhe_ct_mul(hmpc_context* ctx, hmpc_modulus* q, uint64_t elements, const uint32_t* a0, const uint32_t* a1,
+                    const uint32_t* b0, const uint32_t* b1, uint32_t* d0, uint32_t* d1, uint32_t* d2)
+{
     if (int rc = enter(ctx))
     {
         return rc;
     }
-    if (!q || !p || !s || !c0 || !c1 || !out)
+    if (!q || (elements && (!a0 || !a1 || !b0 || !b1 || !d0 || !d1 || !d2)))
     {
         return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
     }
-    if (int rc = check_degree(n))
-    {
-        return rc;
-    }
-    if (batch == 0)
-    {
-        return HMPC_OK;
-    }
-    const uint64_t elements = n * batch;
-    uint32_t* x = ctx->scratch(elements * static_cast<uint64_t>(q->c.limbs));
-    if (!x)
-    {
-        return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating the decryption workspace");
-    }
-    cudaError_t e = q->kt->binary(x, s, n, c1, elements, elements, HMPC_OP_MUL, q->h, ctx->stream);
-    if (e == cudaSuccess)
-    {
-        e = q->kt->binary(x, c0, elements, x, elements, elements, HMPC_OP_SUB, q->h, ctx->stream);
-    }
+    cudaError_t e = q->kt->ct_mul(d0, d1, d2, a0, a1, b0, b1, elements, q->h, ctx->stream);
     if (e != cudaSuccess)
     {
-        return cuda_fail(e, "launching elementwise op");
+        return cuda_fail(e, "launching ciphertext product");
     }
-    ctx->launches += 2;
-    int rc = run_transform(ctx, q, n, batch, true, producer_tensor, 0, 0, x, x);
-    if (rc)
+    ctx->launches += elements ? 1 : 0;
+    return HMPC_OK;
+}
+
+int hmpc_ntt_forward_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch,
+                           const hmpc_producer* producer, uint32_t* out)
+{
+    if (!producer)
     {
-        return rc;
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null producer");
     }
-    e = p->kt->cast(out, x, elements, make_cast(p, q), p->h, ctx->stream);
-    if (e != cudaSuccess)
-    {
-        return cuda_fail(e, "launching cast");
-    }
-    ++ctx->launches;
-    if (plaintext_ntt)
-    {
-        rc = run_transform(ctx, p, n, batch, false, producer_tensor, 0, 0, out, out);
-    }
-    return rc;
+    return run_plain(ctx, mod, n, batch, false, producer->kind, producer->variance_x2, producer->security,
+                     producer->src, out);
+}
+
+int hmpc_ntt_inverse_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const uint32_t* in,
+                           uint32_t* out)
+{
+    return run_plain(ctx, mod, n, batch, true, producer_tensor, 0, 0, in, out);
 }
 
 int hmpc_lhe_keygen(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint32_t* s, uint32_t* a,

@@ -9,6 +9,7 @@
 
 #include "chacha.cuh"
 #include "ntt.cuh"
+#include "plain.cuh"
 
 namespace hmpc_gb300
 {
@@ -62,6 +63,14 @@ namespace hmpc_gb300
                                        cudaStream_t stream);
         cudaError_t (*cast)(uint32_t* out, const uint32_t* in, uint64_t elements, const CastParams& cp,
                             const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*plain_stage)(const PlainStageParams& p, int kind, int nw, const HostModulus& m,
+                                   cudaStream_t stream);
+        cudaError_t (*ct_mul)(uint32_t* d0, uint32_t* d1, uint32_t* d2, const uint32_t* a0, const uint32_t* a1,
+                              const uint32_t* b0, const uint32_t* b1, uint64_t elements, const HostModulus& m,
+                              cudaStream_t stream);
+        cudaError_t (*dec_combine)(uint32_t* x, const uint32_t* s, uint64_t n, const uint32_t* c0,
+                                   const uint32_t* c1, const uint32_t* c2, uint64_t elements, const HostModulus& m,
+                                   cudaStream_t stream);
         int radix_bits;
     };
 

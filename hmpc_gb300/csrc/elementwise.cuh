@@ -168,6 +168,62 @@ namespace hmpc_gb300
         }
     }
 
+    // ciphertext x ciphertext in NTT form: the tensor product
+    // (d0, d1, d2) = (a0*b0, a0*b1 + a1*b0, a1*b1).  No counterpart in the
+    // reference, whose ciphertexts only support linear operations
+    // (expr/crypto/lhe/ciphertext.hpp:49-81).
+    template<int L>
+    __global__ void __launch_bounds__(256) ct_mul_kernel(uint32_t* d0, uint32_t* d1, uint32_t* d2,
+                                                         const uint32_t* a0, const uint32_t* a1, const uint32_t* b0,
+                                                         const uint32_t* b1, uint64_t elements, const Modulus<L> m)
+    {
+        for (uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < elements;
+             e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        {
+            uint32_t x0[L], x1[L], y0[L], y1[L], r[L], t[L];
+            load1<L>(x0, a0, elements, e);
+            load1<L>(x1, a1, elements, e);
+            load1<L>(y0, b0, elements, e);
+            load1<L>(y1, b1, elements, e);
+            mont_mul<L>(r, x0, y0, m);
+            store1<L>(d0, elements, e, r);
+            mont_mul<L>(r, x0, y1, m);
+            mont_mul<L>(t, x1, y0, m);
+            mod_add<L>(r, r, t, m);
+            store1<L>(d1, elements, e, r);
+            mont_mul<L>(r, x1, y1, m);
+            store1<L>(d2, elements, e, r);
+        }
+    }
+
+    // x = c0 - s*c1 (+ s^2*c2 for a product ciphertext), s broadcast over the
+    // batch: the first node of dec (expr/crypto/lhe/dec.hpp:29), extended to
+    // degree-2 ciphertexts by Horner's rule c0 - s*(c1 - s*c2).
+    template<int L>
+    __global__ void __launch_bounds__(256) dec_combine_kernel(uint32_t* x, const uint32_t* s, uint64_t n,
+                                                              const uint32_t* c0, const uint32_t* c1,
+                                                              const uint32_t* c2, uint64_t elements,
+                                                              const Modulus<L> m)
+    {
+        for (uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < elements;
+             e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        {
+            uint32_t sk[L], a[L], b[L];
+            load1<L>(sk, s, n, e % n);
+            load1<L>(b, c1, elements, e);
+            if (c2)
+            {
+                load1<L>(a, c2, elements, e);
+                mont_mul<L>(a, sk, a, m);
+                mod_sub<L>(b, b, a, m);
+            }
+            mont_mul<L>(b, sk, b, m);
+            load1<L>(a, c0, elements, e);
+            mod_sub<L>(a, a, b, m);
+            store1<L>(x, elements, e, a);
+        }
+    }
+
     // elementwise samplers: element e uses the generator (key, nonce,
     // counter = e) and draws one value (expr/random/uniform.hpp:41-45,
     // expr/random/binomial.hpp:207-211, comp/queue.hpp:386-412)

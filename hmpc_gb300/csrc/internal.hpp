@@ -136,5 +136,7 @@ namespace hmpc_gb300::detail
     int enter(hmpc_context* ctx);
     int run_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                       uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
+    int run_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
+                  uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
     CastParams make_cast(const hmpc_modulus* dst, const hmpc_modulus* src);
 }

@@ -229,8 +229,72 @@ namespace hmpc_gb300
             return cudaGetLastError();
         }
 
-        const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd,
-                                   to_montgomery, from_montgomery, cast, R};
+        template<int Kind, int NW>
+        cudaError_t launch_plain(const PlainStageParams& p, const Modulus<L>& m, cudaStream_t stream)
+        {
+            plain_stage_kernel<L, Kind, NW><<<grid_for(p.elements / 2, 256), 256, 0, stream>>>(p, m);
+            return cudaGetLastError();
+        }
+
+        cudaError_t plain_stage(const PlainStageParams& p, int kind, int nw, const HostModulus& h, cudaStream_t stream)
+        {
+            const Modulus<L> m = device_modulus(h);
+            if (kind == producer_tensor || p.stage != 0)
+            {
+                return launch_plain<producer_tensor, 1>(p, m, stream);
+            }
+            if (kind == producer_cbd)
+            {
+                switch (nw)
+                {
+                case 1: return launch_plain<producer_cbd, 1>(p, m, stream);
+                case 2: return launch_plain<producer_cbd, 2>(p, m, stream);
+                case 3: return launch_plain<producer_cbd, 3>(p, m, stream);
+                case 4: return launch_plain<producer_cbd, 4>(p, m, stream);
+                default: return cudaErrorInvalidValue;
+                }
+            }
+            if (kind == producer_uniform)
+            {
+                if (nw == L + 2)
+                {
+                    return launch_plain<producer_uniform, L + 2>(p, m, stream);
+                }
+                if (nw == L + 3)
+                {
+                    return launch_plain<producer_uniform, L + 3>(p, m, stream);
+                }
+            }
+            return cudaErrorInvalidValue;
+        }
+
+        cudaError_t ct_mul(uint32_t* d0, uint32_t* d1, uint32_t* d2, const uint32_t* a0, const uint32_t* a1,
+                           const uint32_t* b0, const uint32_t* b1, uint64_t elements, const HostModulus& h,
+                           cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            ct_mul_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(d0, d1, d2, a0, a1, b0, b1, elements,
+                                                                          device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t dec_combine(uint32_t* x, const uint32_t* s, uint64_t n, const uint32_t* c0, const uint32_t* c1,
+                                const uint32_t* c2, uint64_t elements, const HostModulus& h, cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            dec_combine_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(x, s, n, c0, c1, c2, elements,
+                                                                               device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd, to_montgomery,
+                                   from_montgomery, cast, plain_stage, ct_mul, dec_combine, R};
     }
 
     const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()

@@ -158,60 +158,76 @@ namespace hmpc_gb300
     }
 
     template<int L>
-    __device__ __forceinline__ void load_twiddle(uint32_t (&t)[L], const uint32_t* table, uint64_t index)
+    __device__ __forceinline__ void load_twiddle(uint32_t (&t)[L], const uint32_t* table, uint32_t index)
     {
-#pragma unroll
-        for (int j = 0; j < L; ++j)
+        const uint32_t* ptr = table + static_cast<size_t>(index) * L;
+        if constexpr (L % 4 == 0)
         {
-            t[j] = __ldg(table + index * L + j);
+#pragma unroll
+            for (int j = 0; j < L; j += 4)
+            {
+                const uint4 v = __ldg(reinterpret_cast<const uint4*>(ptr + j));
+                t[j] = v.x;
+                t[j + 1] = v.y;
+                t[j + 2] = v.z;
+                t[j + 3] = v.w;
+            }
+        }
+        else if constexpr (L % 2 == 0)
+        {
+#pragma unroll
+            for (int j = 0; j < L; j += 2)
+            {
+                const uint2 v = __ldg(reinterpret_cast<const uint2*>(ptr + j));
+                t[j] = v.x;
+                t[j + 1] = v.y;
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int j = 0; j < L; ++j)
+            {
+                t[j] = __ldg(ptr + j);
+            }
         }
     }
 
     // One pass over the tiles of a batch.  R = register bits per thread.
+    // The first register group reads its elements straight from global memory
+    // (or generates them), the last one writes them straight back; the groups
+    // in between exchange data through shared memory.  Register bits always
+    // lie inside one tile (the planner keeps c + w >= R), so a register
+    // block's element indices are its base index plus fixed offsets.
     template<int L, int R, int Kind, int NW>
-    __global__ void __launch_bounds__(256) ntt_pass_kernel(const NttPassParams p, const Modulus<L> m)
+    __global__ void __launch_bounds__(256, 2) ntt_pass_kernel(const NttPassParams p, const Modulus<L> m)
     {
         extern __shared__ uint32_t smem[];
         constexpr int regs = 1 << R;
         const uint32_t local_count = 1u << p.local_bits;
         const uint32_t limb_stride = smem_addr(local_count);
         const uint32_t w = p.s1 - p.s0;
+        const uint32_t c = p.col_bits;
+        const uint32_t log_n = p.log_n;
+        const uint64_t n = 1ull << log_n;
 
         NttTileGeometry<L> geo;
         geo.w = w;
-        geo.c = p.col_bits;
+        geo.c = c;
         geo.tile_bits = p.tile_bits;
         geo.rs = p.row_shift;
-        geo.log_n = p.log_n;
-        geo.n = 1ull << p.log_n;
+        geo.log_n = log_n;
+        geo.n = n;
         geo.tile0 = static_cast<uint64_t>(blockIdx.x) << p.tile_bits;
 
-        const bool fused = Kind != producer_tensor;
-        if (!fused)
-        {
-            const uint32_t* in = p.src ? p.src : p.out;
-            for (uint32_t local = threadIdx.x; local < local_count; local += blockDim.x)
-            {
-                if (geo.tile_of(local) >= p.tiles)
-                {
-                    continue;  // partial last CTA: nothing to load, nothing is stored
-                }
-                uint64_t poly, idx;
-                geo.locate(local, poly, idx);
-                const uint64_t e = poly * geo.n + idx;
-#pragma unroll
-                for (int j = 0; j < L; ++j)
-                {
-                    smem[j * limb_stride + smem_addr(local)] = in[static_cast<uint64_t>(j) * p.elements + e];
-                }
-            }
-            __syncthreads();
-        }
-
+        const uint32_t* in = p.src ? p.src : p.out;
+        const uint32_t blocks = local_count >> R;
+        const uint32_t last = p.num_groups - 1;
         for (uint32_t gi = 0; gi < p.num_groups; ++gi)
         {
             const NttGroup& g = p.groups[gi];
-            uint32_t off[regs];
+            uint32_t off[regs];    // CTA-local offset of register x
+            uint32_t eoff[regs];   // offset of register x inside its polynomial
 #pragma unroll
             for (int x = 0; x < regs; ++x)
             {
@@ -225,22 +241,43 @@ namespace hmpc_gb300
                     }
                 }
                 off[x] = o;
+                eoff[x] = (o & ((1u << c) - 1u)) | ((o >> c) << p.row_shift);
             }
-            const uint32_t blocks = local_count >> R;
             for (uint32_t b = threadIdx.x; b < blocks; b += blockDim.x)
             {
                 const uint32_t base = deposit_bits(b, g.rest_mask);
-                uint32_t x_reg[regs][L];
-                if (fused && gi == 0)
+                if (geo.tile_of(base) >= p.tiles)
                 {
-                    // stage 0 pairs register bit 0: (x, x | 1)
-#pragma unroll
-                    for (int x = 0; x < regs; x += 2)
+                    continue;  // partial last CTA: nothing to load or store
+                }
+                uint64_t poly, idx64;
+                geo.locate(base, poly, idx64);
+                const uint32_t idx = static_cast<uint32_t>(idx64);
+                const uint64_t ebase = poly * n + idx;
+                uint32_t x_reg[regs][L];
+                if (gi == 0)
+                {
+                    if constexpr (Kind != producer_tensor)
                     {
-                        uint64_t poly, idx_u, idx_v;
-                        geo.locate(base | off[x], poly, idx_u);
-                        geo.locate(base | off[x | 1], poly, idx_v);
-                        produce_pair<L, Kind, NW>(p, m, poly, idx_u, idx_v, x_reg[x], x_reg[x | 1]);
+                        // stage 0 pairs register bit 0: (x, x | 1)
+#pragma unroll
+                        for (int x = 0; x < regs; x += 2)
+                        {
+                            produce_pair<L, Kind, NW>(p, m, poly, idx + eoff[x], idx + eoff[x | 1], x_reg[x],
+                                                      x_reg[x | 1]);
+                        }
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int x = 0; x < regs; ++x)
+                        {
+#pragma unroll
+                            for (int j = 0; j < L; ++j)
+                            {
+                                x_reg[x][j] = in[static_cast<uint64_t>(j) * p.elements + ebase + eoff[x]];
+                            }
+                        }
                     }
                 }
                 else
@@ -262,18 +299,17 @@ namespace hmpc_gb300
                     if (static_cast<uint32_t>(k) < g.count)
                     {
                         const uint32_t s = g.stage + k;
-                        const bool last_inverse = p.inverse && s == p.log_n - 1;
+                        const bool last_inverse = p.inverse && s == log_n - 1;
 #pragma unroll
                         for (int x = 0; x < regs; ++x)
                         {
                             if ((x & (1 << k)) == 0)
                             {
-                                uint64_t poly, idx;
-                                geo.locate(base | off[x], poly, idx);
+                                const uint32_t e = idx + eoff[x];  // lower element of the pair
                                 uint32_t t[L];
                                 if (!p.inverse)
                                 {
-                                    load_twiddle<L>(t, p.twiddles, (1ull << s) + (idx >> (p.log_n - s)));
+                                    load_twiddle<L>(t, p.twiddles, (1u << s) + (e >> (log_n - s)));
                                     mont_mul<L>(x_reg[x | (1 << k)], x_reg[x | (1 << k)], t, m);
                                     uint32_t sum[L];
                                     mod_add<L>(sum, x_reg[x], x_reg[x | (1 << k)], m);
@@ -286,7 +322,7 @@ namespace hmpc_gb300
                                 }
                                 else if (!last_inverse)
                                 {
-                                    load_twiddle<L>(t, p.twiddles, (geo.n >> (s + 1)) + (idx >> (s + 1)));
+                                    load_twiddle<L>(t, p.twiddles, static_cast<uint32_t>(n >> (s + 1)) + (e >> (s + 1)));
                                     uint32_t sum[L], diff[L];
                                     mod_add<L>(sum, x_reg[x], x_reg[x | (1 << k)], m);
                                     mod_sub<L>(diff, x_reg[x], x_reg[x | (1 << k)], m);
@@ -302,42 +338,44 @@ namespace hmpc_gb300
                                     uint32_t sum[L], diff[L];
                                     mod_add<L>(sum, x_reg[x], x_reg[x | (1 << k)], m);
                                     mod_sub<L>(diff, x_reg[x], x_reg[x | (1 << k)], m);
-                                    load_twiddle<L>(t, p.twiddles, 0);
+                                    load_twiddle<L>(t, p.twiddles, 0u);
                                     mont_mul<L>(x_reg[x], sum, t, m);
-                                    load_twiddle<L>(t, p.twiddles, 1);
+                                    load_twiddle<L>(t, p.twiddles, 1u);
                                     mont_mul<L>(x_reg[x | (1 << k)], diff, t, m);
                                 }
                             }
                         }
                     }
                 }
-#pragma unroll
-                for (int x = 0; x < regs; ++x)
+                if (gi == last)
                 {
-                    const uint32_t a = smem_addr(base | off[x]);
 #pragma unroll
-                    for (int j = 0; j < L; ++j)
+                    for (int x = 0; x < regs; ++x)
                     {
-                        smem[j * limb_stride + a] = x_reg[x][j];
+#pragma unroll
+                        for (int j = 0; j < L; ++j)
+                        {
+                            p.out[static_cast<uint64_t>(j) * p.elements + ebase + eoff[x]] = x_reg[x][j];
+                        }
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int x = 0; x < regs; ++x)
+                    {
+                        const uint32_t a = smem_addr(base | off[x]);
+#pragma unroll
+                        for (int j = 0; j < L; ++j)
+                        {
+                            smem[j * limb_stride + a] = x_reg[x][j];
+                        }
                     }
                 }
             }
-            __syncthreads();
-        }
-
-        for (uint32_t local = threadIdx.x; local < local_count; local += blockDim.x)
-        {
-            if (geo.tile_of(local) >= p.tiles)
+            if (gi != last)
             {
-                continue;
-            }
-            uint64_t poly, idx;
-            geo.locate(local, poly, idx);
-            const uint64_t e = poly * geo.n + idx;
-#pragma unroll
-            for (int j = 0; j < L; ++j)
-            {
-                p.out[static_cast<uint64_t>(j) * p.elements + e] = smem[j * limb_stride + smem_addr(local)];
+                __syncthreads();
             }
         }
     }

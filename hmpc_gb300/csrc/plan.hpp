@@ -72,11 +72,26 @@ namespace hmpc_gb300
         return r;
     }
 
+    // every pass must hold at least one full register group inside a tile
+    // (c + w >= R); shrink the column pass above a too-narrow final pass
+    inline void keep_register_groups(std::vector<BitRange>& r, int R, int b)
+    {
+        if (r.size() >= 2 && r.back().hi < R)
+        {
+            BitRange& prev = r[r.size() - 2];
+            const int grow = R - r.back().hi;
+            prev.lo += grow;
+            prev.c = std::min(std::min(b - (prev.hi - prev.lo), prev.lo), 5);
+            r.back().hi += grow;
+        }
+    }
+
     inline std::vector<PassPlan> plan_transform(int limbs, int log_n, uint64_t batch, bool inverse, int R,
                                                 const PlanOptions& o = {})
     {
         const int b = local_bits_for(limbs, o);
         std::vector<BitRange> ranges = plan_ranges(log_n, b, o.col_bits);
+        keep_register_groups(ranges, R, b);
         if (inverse)
         {
             std::reverse(ranges.begin(), ranges.end());
