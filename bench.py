@@ -173,6 +173,88 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def hbm_peak_gbs():
+    """measured copy bandwidth of the GB300s (driver-written), else the
+    fallback figure"""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def secondary_metrics(queue, int_peak):
+    """The other configurations' measurements (parity is in tests/): FMA over
+    2^24 residues (HBM-bound), one N=4096 NTT+INTT (latency), and the batched
+    uneven-degree NTT (512 polynomials, q 192-bit) against one plain call per
+    polynomial."""
+    import torch
+
+    from hmpc_gb300.batch import NttBatch, uneven_degrees
+    from hmpc_gb300.comp import Tensor
+    from hmpc_gb300.workloads import MODULI
+
+    out = {}
+    stream = queue.stream
+
+    def time_ms(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    # FMA, 2^24 residues of 4 limbs: 3 reads + 1 write of 16 B
+    peak, source = hbm_peak_gbs()
+    qf = queue.modulus(MODULI["fma"])
+    count = 1 << 24
+    a, b, c = (queue.uniform(qf, (count,)) for _ in range(3))
+    d = Tensor(qf, (count,))
+    ms = time_ms(lambda: queue.fma(a, b, c, out=d), 20)
+    gbs = count * 64 / (ms * 1e-3) / 1e9
+    out["fma_2^24_L4"] = {"ms": ms, "GB/s": gbs, "hbm_frac": gbs / peak, "hbm_peak_source": source}
+    del a, b, c, d
+
+    # single transform N = 4096, q 125-bit (examples/ntt.cpp modulus), batch 1
+    qn = queue.modulus(MODULI["ntt"])
+    qn.prepare(4096)
+    x = queue.uniform(qn, (1,), 4096)
+    y = Tensor(qn, (1,), 4096)
+    z = Tensor(qn, (1,), 4096)
+    ms_tiled = time_ms(lambda: (queue.ntt(x, out=y), queue.intt(y, out=z)), 200)
+    ms_plain = time_ms(lambda: (queue.ntt_plain(x, out=y), queue.ntt_plain(y, out=z, inverse=True)), 200)
+    out["ntt_intt_4096_L4_batch1"] = {"us_tiled": ms_tiled * 1e3, "us_plain": ms_plain * 1e3}
+
+    # batched uneven degrees: one persistent graph launch vs one plain call per polynomial
+    degrees = uneven_degrees(512)
+    qb = queue.modulus(MODULI["q192"])
+    xs = [queue.uniform(qb, (), n) for n in degrees]
+    ys = [Tensor(qb, (), n) for n in degrees]
+    batch = NttBatch(queue, qb, degrees, autotune=True)
+    ms_batch = time_ms(lambda: batch.run(xs, ys), 10)
+    ms_calls = time_ms(lambda: [queue.ntt(xi, out=yi) for xi, yi in zip(xs, ys)], 3)
+    ms_plain = time_ms(lambda: [queue.ntt_plain(xi, out=yi) for xi, yi in zip(xs, ys)], 3)
+    coeffs = sum(degrees)
+    butterflies = sum(n // 2 * (n.bit_length() - 1) for n in degrees)
+    bytes_moved = coeffs * qb.limbs * 4 * 2
+    ops = butterflies * mont_mul_ops(qb.limbs)
+    out["batched_ntt_512_uneven_L6"] = {
+        "ms": ms_batch,
+        "coefficients_per_s": coeffs / (ms_batch * 1e-3),
+        "GB/s": bytes_moved / (ms_batch * 1e-3) / 1e9,
+        "int_frac": ops / (ms_batch * 1e-3) / int_peak,
+        "vs_plain_per_polynomial_calls": ms_plain / ms_batch,
+        "vs_tiled_per_polynomial_calls": ms_calls / ms_batch,
+        "ms_plain_per_polynomial_calls": ms_plain,
+        "tile": batch.info(),
+    }
+    batch.close()
+    return out
+
+
 def cpu_baseline_sample():
     from oracle import oracle
 
@@ -203,6 +285,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -357,6 +440,8 @@ def main():
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
+        if not args.no_secondary:
+            line["secondary"] = secondary_metrics(queue, peak)
         print(json.dumps(line), flush=True)
     queue.close()
     if world > 1:

@@ -68,6 +68,16 @@ SIGNATURES = {
     "hmpc_tensor_download": ([_vp, _vp, _vp, _u64], _int),
     "hmpc_ntt_forward": ([_vp, _vp, _u64, _u64, ctypes.POINTER(Producer), _vp], _int),
     "hmpc_ntt_inverse": ([_vp, _vp, _u64, _u64, _vp, _vp], _int),
+    "hmpc_ntt_forward_plain": ([_vp, _vp, _u64, _u64, ctypes.POINTER(Producer), _vp], _int),
+    "hmpc_ntt_inverse_plain": ([_vp, _vp, _u64, _u64, _vp, _vp], _int),
+    "hmpc_lhe_dec2": ([_vp, _vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _int, _vp], _int),
+    "hmpc_lhe_ct_mul": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp], _int),
+    "hmpc_ntt_batch_create": ([_vp, _vp, _u64, ctypes.POINTER(_u64), _int, _int, ctypes.POINTER(_vp)], _int),
+    "hmpc_ntt_batch_run": ([_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)], _int),
+    "hmpc_ntt_batch_info": ([_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_int),
+                             ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_float)], _int),
+    "hmpc_ntt_batch_status": ([_vp, ctypes.POINTER(ctypes.c_uint32)], _int),
+    "hmpc_ntt_batch_destroy": ([_vp], _int),
     "hmpc_fma": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp], _int),
     "hmpc_binary": ([_vp, _vp, _int, _u64, _vp, _u64, _vp, _u64, _vp], _int),
     "hmpc_sample_uniform": ([_vp, _vp, _u64, ctypes.c_uint32, _vp], _int),

@@ -197,6 +197,24 @@ class Queue:
         _lib.call("hmpc_ntt_forward", self.handle, modulus.handle, n, out.batch, ctypes.byref(prod), out.ptr())
         return out
 
+    def ntt_plain(self, x, out=None, inverse=False):
+        """the per-stage comparator transform (one launch per stage)"""
+        out = out or make_tensor(x.modulus, x.shape, x.n)
+        if inverse:
+            _lib.call("hmpc_ntt_inverse_plain", self.handle, x.modulus.handle, x.n, x.batch, x.ptr(), out.ptr())
+        else:
+            prod = _lib.Producer(_lib.PRODUCER_TENSOR, x.data.data_ptr(), 0, 0)
+            _lib.call("hmpc_ntt_forward_plain", self.handle, x.modulus.handle, x.n, x.batch, ctypes.byref(prod),
+                      out.ptr())
+        return out
+
+    def ntt_plain_centered_binomial(self, modulus, n, shape, variance_x2, out=None):
+        out = out or make_tensor(modulus, shape, n)
+        prod = _lib.Producer(_lib.PRODUCER_CBD, None, variance_x2, 0)
+        _lib.call("hmpc_ntt_forward_plain", self.handle, modulus.handle, n, out.batch, ctypes.byref(prod),
+                  out.ptr())
+        return out
+
     # ----------------------------------------------------------- elementwise
     def fma(self, a, b, c, out=None):
         out = out or make_tensor(a.modulus, a.shape, a.n)

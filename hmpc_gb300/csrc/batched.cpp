@@ -1,0 +1,502 @@
+// Batched transforms of polynomials of uneven degree: one persistent kernel
+// launch per batch, replayed from a captured CUDA graph, with the tile shape
+// (register radix, stages per shared-memory pass, coalescing columns) chosen
+// by timing candidates on the device.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "internal.hpp"
+#include "plan.hpp"
+
+using namespace hmpc_gb300;
+using namespace hmpc_gb300::detail;
+
+struct hmpc_ntt_batch
+{
+    hmpc_context* ctx = nullptr;
+    hmpc_modulus* mod = nullptr;
+    bool inverse = false;
+    std::vector<uint64_t> degrees;
+
+    // chosen configuration
+    int radix_bits = 3;
+    int local_bits = 0;
+    int col_bits = 4;
+    float tuned_ms = 0.f;
+
+    // plan
+    std::vector<NttPassParams> params;        // host copy (pointers rebound per run)
+    std::vector<uint32_t> param_poly;         // params index -> polynomial
+    std::vector<uint32_t> param_pass;         // params index -> pass
+    uint32_t items = 0;
+    size_t smem = 0;
+    unsigned grid = 0;
+
+    // device state
+    NttPassParams* d_params = nullptr;
+    uint32_t* d_items = nullptr;               // 5 arrays of `items` words
+    uint32_t* d_counters = nullptr;            // one per polynomial + control block
+    NttPassParams* h_params = nullptr;         // pinned staging
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t start = nullptr, finish = nullptr;
+    std::vector<const uint32_t*> bound_in;
+    std::vector<uint32_t*> bound_out;
+
+    void release_plan()
+    {
+        if (exec)
+        {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+        cudaFree(d_params);
+        cudaFree(d_items);
+        cudaFree(d_counters);
+        cudaFreeHost(h_params);
+        d_params = nullptr;
+        d_items = nullptr;
+        d_counters = nullptr;
+        h_params = nullptr;
+        bound_in.clear();
+        bound_out.clear();
+    }
+
+    ~hmpc_ntt_batch()
+    {
+        if (stream)
+        {
+            cudaStreamSynchronize(stream);
+        }
+        release_plan();
+        if (start)
+        {
+            cudaEventDestroy(start);
+        }
+        if (finish)
+        {
+            cudaEventDestroy(finish);
+        }
+        if (stream)
+        {
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    BatchedControl* control() const
+    {
+        return reinterpret_cast<BatchedControl*>(d_counters + degrees.size());
+    }
+
+    // Build the work list and device arrays for one configuration.
+    int build(int R, int b, int c_pref)
+    {
+        release_plan();
+        radix_bits = R;
+        local_bits = b;
+        col_bits = c_pref;
+        const int L = mod->c.limbs;
+        PlanOptions o;
+        o.max_local_bits = b;
+        o.col_bits = c_pref;
+        o.spread_small_batches = false;
+        params.clear();
+        param_poly.clear();
+        param_pass.clear();
+        std::vector<std::vector<PassPlan>> plans(degrees.size());
+        size_t max_passes = 0;
+        smem = 0;
+        for (size_t i = 0; i < degrees.size(); ++i)
+        {
+            Tables* t = nullptr;
+            if (int rc = mod->prepare(degrees[i], &t))
+            {
+                return rc;
+            }
+            plans[i] = plan_transform(L, __builtin_ctzll(degrees[i]), 1, inverse, R, o);
+            max_passes = std::max(max_passes, plans[i].size());
+            for (const PassPlan& pp : plans[i])
+            {
+                smem = std::max(smem, pp.smem);
+            }
+        }
+        if (smem > 200 * 1024)
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "tile configuration exceeds shared memory");
+        }
+        // params index of (poly, pass); items: every pass-0 item first, larger
+        // polynomials first, then pass 1, ...
+        std::vector<std::vector<uint32_t>> index(degrees.size());
+        for (size_t i = 0; i < degrees.size(); ++i)
+        {
+            Tables* t = nullptr;
+            mod->prepare(degrees[i], &t);
+            for (size_t k = 0; k < plans[i].size(); ++k)
+            {
+                NttPassParams p = plans[i][k].params;
+                p.twiddles = inverse ? t->inverse : t->forward;
+                p.small_table = mod->small_table;
+                p.elements = degrees[i];
+                p.out = nullptr;
+                p.src = nullptr;
+                index[i].push_back(static_cast<uint32_t>(params.size()));
+                params.push_back(p);
+                param_poly.push_back(static_cast<uint32_t>(i));
+                param_pass.push_back(static_cast<uint32_t>(k));
+            }
+        }
+        std::vector<uint32_t> order(degrees.size());
+        std::iota(order.begin(), order.end(), 0u);
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b2) { return degrees[a] > degrees[b2]; });
+        std::vector<uint32_t> item_param, item_tile, item_wait, item_poly, item_signal;
+        for (size_t k = 0; k < max_passes; ++k)
+        {
+            for (uint32_t i : order)
+            {
+                if (k >= plans[i].size())
+                {
+                    continue;
+                }
+                uint32_t before = 0;
+                for (size_t j = 0; j < k; ++j)
+                {
+                    before += plans[i][j].grid;
+                }
+                for (unsigned g = 0; g < plans[i][k].grid; ++g)
+                {
+                    item_param.push_back(index[i][k]);
+                    item_tile.push_back(g);
+                    item_wait.push_back(before);
+                    item_poly.push_back(i);
+                    item_signal.push_back(k + 1 < plans[i].size() ? 1u : 0u);
+                }
+            }
+        }
+        items = static_cast<uint32_t>(item_param.size());
+        const size_t pbytes = params.size() * sizeof(NttPassParams);
+        HMPC_CUDA(cudaMalloc(&d_params, pbytes), "allocating batch parameters");
+        HMPC_CUDA(cudaMallocHost(&h_params, pbytes), "allocating batch parameters");
+        std::memcpy(h_params, params.data(), pbytes);
+        HMPC_CUDA(cudaMalloc(&d_items, 5ull * items * sizeof(uint32_t)), "allocating work list");
+        HMPC_CUDA(cudaMalloc(&d_counters, (degrees.size() + 4) * sizeof(uint32_t)), "allocating counters");
+        std::vector<uint32_t> packed;
+        for (auto* v : {&item_param, &item_tile, &item_wait, &item_poly, &item_signal})
+        {
+            packed.insert(packed.end(), v->begin(), v->end());
+        }
+        HMPC_CUDA(cudaMemcpy(d_items, packed.data(), packed.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+                  "uploading work list");
+        int sms = 0;
+        HMPC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "querying SMs");
+        const int per_sm = std::max(1, mod->kt->ntt_batched_blocks_per_sm(R, smem));
+        grid = static_cast<unsigned>(std::min<uint64_t>(items, static_cast<uint64_t>(sms) * per_sm));
+        // graph: reset counters and control, then the persistent kernel
+        BatchedParams bp{};
+        bp.params = d_params;
+        bp.item_param = d_items;
+        bp.item_tile = d_items + items;
+        bp.item_wait = d_items + 2ull * items;
+        bp.item_poly = d_items + 3ull * items;
+        bp.item_signal = d_items + 4ull * items;
+        bp.counters = d_counters;
+        bp.control = control();
+        bp.items = items;
+        bp.spin_limit = 1u << 24;  // ~1 s of 64 ns polls
+        cudaGraph_t graph = nullptr;
+        HMPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capturing batch graph");
+        cudaError_t e = cudaMemsetAsync(d_counters, 0, (degrees.size() + 4) * sizeof(uint32_t), stream);
+        if (e == cudaSuccess)
+        {
+            e = mod->kt->ntt_batched(bp, R, mod->h, grid, smem, stream);
+        }
+        cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess)
+        {
+            if (graph)
+            {
+                cudaGraphDestroy(graph);
+            }
+            return cuda_fail(e != cudaSuccess ? e : e2, "capturing batch graph");
+        }
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "instantiating batch graph");
+        }
+        return HMPC_OK;
+    }
+
+    int bind(const uint32_t* const* in, uint32_t* const* out)
+    {
+        bool same = bound_in.size() == degrees.size();
+        for (size_t i = 0; same && i < degrees.size(); ++i)
+        {
+            same = bound_in[i] == in[i] && bound_out[i] == out[i];
+        }
+        if (same)
+        {
+            return HMPC_OK;
+        }
+        // the staging buffer may still feed the previous copy
+        HMPC_CUDA(cudaStreamSynchronize(stream), "waiting for the previous batch");
+        for (size_t k = 0; k < params.size(); ++k)
+        {
+            const uint32_t i = param_poly[k];
+            h_params[k].out = out[i];
+            h_params[k].src = param_pass[k] == 0 ? in[i] : nullptr;
+        }
+        HMPC_CUDA(cudaMemcpyAsync(d_params, h_params, params.size() * sizeof(NttPassParams), cudaMemcpyHostToDevice,
+                                  stream),
+                  "uploading batch pointers");
+        bound_in.assign(in, in + degrees.size());
+        bound_out.assign(out, out + degrees.size());
+        return HMPC_OK;
+    }
+
+    int launch(const uint32_t* const* in, uint32_t* const* out)
+    {
+        HMPC_CUDA(cudaEventRecord(start, ctx->stream), "ordering batch");
+        HMPC_CUDA(cudaStreamWaitEvent(stream, start, 0), "ordering batch");
+        if (int rc = bind(in, out))
+        {
+            return rc;
+        }
+        HMPC_CUDA(cudaGraphLaunch(exec, stream), "launching batch graph");
+        HMPC_CUDA(cudaEventRecord(finish, stream), "ordering batch");
+        HMPC_CUDA(cudaStreamWaitEvent(ctx->stream, finish, 0), "ordering batch");
+        ++ctx->launches;
+        return HMPC_OK;
+    }
+};
+
+namespace
+{
+    // time one configuration on scratch buffers (the transform's cost does
+    // not depend on the values)
+    float time_config(hmpc_ntt_batch* b, const std::vector<const uint32_t*>& in, const std::vector<uint32_t*>& out)
+    {
+        cudaEvent_t t0, t1;
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        float best = 1e30f;
+        for (int rep = 0; rep < 5; ++rep)
+        {
+            cudaEventRecord(t0, b->ctx->stream);
+            if (b->launch(in.data(), out.data()) != HMPC_OK)
+            {
+                best = 1e30f;
+                break;
+            }
+            cudaEventRecord(t1, b->ctx->stream);
+            cudaEventSynchronize(t1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (rep >= 1)
+            {
+                best = std::min(best, ms);
+            }
+        }
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        return best;
+    }
+}
+
+extern "C" {
+
+int hmpc_ntt_batch_create(hmpc_context* ctx, hmpc_modulus* mod, uint64_t count, const uint64_t* degrees, int inverse,
+                          int autotune, hmpc_ntt_batch** out)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!mod || !degrees || !out || count == 0)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "empty batch or null argument");
+    }
+    auto* b = new hmpc_ntt_batch;
+    b->ctx = ctx;
+    b->mod = mod;
+    b->inverse = inverse != 0;
+    b->degrees.assign(degrees, degrees + count);
+    for (uint64_t n : b->degrees)
+    {
+        if (int rc = check_degree(n))
+        {
+            delete b;
+            return rc;
+        }
+        if (__builtin_ctzll(n) < 3)
+        {
+            delete b;
+            return fail(HMPC_ERROR_UNSUPPORTED, "batched transforms need degree >= 8");
+        }
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+    {
+        e = cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaEventCreateWithFlags(&b->finish, cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess)
+    {
+        delete b;
+        return cuda_fail(e, "creating the batch stream");
+    }
+    const int L = mod->c.limbs;
+    PlanOptions def;
+    const int b_default = local_bits_for(L, def);
+    int best_r = 3, best_b = b_default, best_c = 4;
+    if (autotune)
+    {
+        // scratch buffers for the trial runs
+        std::vector<uint32_t*> bufs;
+        std::vector<const uint32_t*> ins;
+        bool ok = true;
+        for (uint64_t n : b->degrees)
+        {
+            uint32_t* p = nullptr;
+            if (cudaMalloc(&p, n * static_cast<uint64_t>(L) * sizeof(uint32_t)) != cudaSuccess)
+            {
+                ok = false;
+                break;
+            }
+            cudaMemsetAsync(p, 0, n * static_cast<uint64_t>(L) * sizeof(uint32_t), ctx->stream);
+            bufs.push_back(p);
+            ins.push_back(p);
+        }
+        float best = 1e30f;
+        if (ok)
+        {
+            for (int R : {3, 2})
+            {
+                for (int lb : {b_default - 1, b_default, b_default + 1})
+                {
+                    for (int c : {3, 4, 5})
+                    {
+                        if (lb < 8 || static_cast<uint64_t>(L) * 4u * smem_words(1u << lb) > 200 * 1024)
+                        {
+                            continue;
+                        }
+                        if (b->build(R, lb, c) != HMPC_OK)
+                        {
+                            continue;
+                        }
+                        const float ms = time_config(b, ins, bufs);
+                        if (ms < best)
+                        {
+                            best = ms;
+                            best_r = R;
+                            best_b = lb;
+                            best_c = c;
+                        }
+                    }
+                }
+            }
+        }
+        cudaStreamSynchronize(b->stream);
+        for (auto* p : bufs)
+        {
+            cudaFree(p);
+        }
+        b->tuned_ms = best < 1e29f ? best : 0.f;
+    }
+    if (int rc = b->build(best_r, best_b, best_c))
+    {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return HMPC_OK;
+}
+
+int hmpc_ntt_batch_run(hmpc_ntt_batch* batch, const uint32_t* const* in, uint32_t* const* out)
+{
+    if (!batch || !in || !out)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = enter(batch->ctx))
+    {
+        return rc;
+    }
+    for (size_t i = 0; i < batch->degrees.size(); ++i)
+    {
+        if (!in[i] || !out[i])
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null polynomial buffer");
+        }
+    }
+    return batch->launch(in, out);
+}
+
+int hmpc_ntt_batch_info(const hmpc_ntt_batch* batch, int* radix_bits, int* local_bits, int* col_bits, uint32_t* items,
+                        float* tuned_ms)
+{
+    if (!batch)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null batch");
+    }
+    if (radix_bits)
+    {
+        *radix_bits = batch->radix_bits;
+    }
+    if (local_bits)
+    {
+        *local_bits = batch->local_bits;
+    }
+    if (col_bits)
+    {
+        *col_bits = batch->col_bits;
+    }
+    if (items)
+    {
+        *items = batch->items;
+    }
+    if (tuned_ms)
+    {
+        *tuned_ms = batch->tuned_ms;
+    }
+    return HMPC_OK;
+}
+
+int hmpc_ntt_batch_status(hmpc_ntt_batch* batch, uint32_t* failed_item)
+{
+    if (!batch || !failed_item)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = enter(batch->ctx))
+    {
+        return rc;
+    }
+    BatchedControl control{};
+    HMPC_CUDA(cudaStreamSynchronize(batch->stream), "waiting for the batch");
+    HMPC_CUDA(cudaMemcpy(&control, batch->control(), sizeof control, cudaMemcpyDeviceToHost), "reading batch status");
+    *failed_item = control.error;
+    if (control.error || control.done != batch->items)
+    {
+        return fail(HMPC_ERROR_TIMEOUT, "a batched transform wait ran out; the outputs are incomplete");
+    }
+    return HMPC_OK;
+}
+
+int hmpc_ntt_batch_destroy(hmpc_ntt_batch* batch)
+{
+    if (batch)
+    {
+        cudaSetDevice(batch->ctx->device);
+        delete batch;
+    }
+    return HMPC_OK;
+}
+
+}  // extern "C"

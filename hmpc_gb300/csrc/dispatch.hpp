@@ -71,6 +71,10 @@ namespace hmpc_gb300
         cudaError_t (*dec_combine)(uint32_t* x, const uint32_t* s, uint64_t n, const uint32_t* c0,
                                    const uint32_t* c1, const uint32_t* c2, uint64_t elements, const HostModulus& m,
                                    cudaStream_t stream);
+        // persistent batched transform with R = radix_bits register bits (2 or 3)
+        cudaError_t (*ntt_batched)(const BatchedParams& bp, int radix_bits, const HostModulus& m, unsigned grid,
+                                   size_t smem, cudaStream_t stream);
+        int (*ntt_batched_blocks_per_sm)(int radix_bits, size_t smem);
         int radix_bits;
     };
 

@@ -293,8 +293,51 @@ namespace hmpc_gb300
             return cudaGetLastError();
         }
 
+        template<int RB>
+        cudaError_t launch_batched(const BatchedParams& bp, const Modulus<L>& m, unsigned grid, size_t smem,
+                                   cudaStream_t stream)
+        {
+            // the shared-memory attribute is set by ntt_batched_blocks_per_sm, which
+            // the batch planner calls before it captures this launch
+            ntt_batched_kernel<L, RB><<<grid, 256, smem, stream>>>(bp, m);
+            return cudaGetLastError();
+        }
+
+        cudaError_t ntt_batched(const BatchedParams& bp, int radix_bits, const HostModulus& h, unsigned grid,
+                                size_t smem, cudaStream_t stream)
+        {
+            const Modulus<L> m = device_modulus(h);
+            if (radix_bits == 2)
+            {
+                return launch_batched<2>(bp, m, grid, smem, stream);
+            }
+            if (radix_bits == 3)
+            {
+                return launch_batched<3>(bp, m, grid, smem, stream);
+            }
+            return cudaErrorInvalidValue;
+        }
+
+        int ntt_batched_blocks_per_sm(int radix_bits, size_t smem)
+        {
+            int blocks = 0;
+            cudaError_t e;
+            if (radix_bits == 2)
+            {
+                cudaFuncSetAttribute(ntt_batched_kernel<L, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, ntt_batched_kernel<L, 2>, 256, smem);
+            }
+            else
+            {
+                cudaFuncSetAttribute(ntt_batched_kernel<L, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, ntt_batched_kernel<L, 3>, 256, smem);
+            }
+            return e == cudaSuccess ? blocks : 0;
+        }
+
         const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd, to_montgomery,
-                                   from_montgomery, cast, plain_stage, ct_mul, dec_combine, R};
+                                   from_montgomery, cast, plain_stage, ct_mul, dec_combine, ntt_batched,
+                                   ntt_batched_blocks_per_sm, R};
     }
 
     const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()

@@ -200,9 +200,9 @@ namespace hmpc_gb300
     // lie inside one tile (the planner keeps c + w >= R), so a register
     // block's element indices are its base index plus fixed offsets.
     template<int L, int R, int Kind, int NW>
-    __global__ void __launch_bounds__(256, 2) ntt_pass_kernel(const NttPassParams p, const Modulus<L> m)
+    __device__ __forceinline__ void ntt_process(const NttPassParams& p, const Modulus<L>& m, uint64_t tile0,
+                                                uint32_t* smem)
     {
-        extern __shared__ uint32_t smem[];
         constexpr int regs = 1 << R;
         const uint32_t local_count = 1u << p.local_bits;
         const uint32_t limb_stride = smem_addr(local_count);
@@ -218,7 +218,7 @@ namespace hmpc_gb300
         geo.rs = p.row_shift;
         geo.log_n = log_n;
         geo.n = n;
-        geo.tile0 = static_cast<uint64_t>(blockIdx.x) << p.tile_bits;
+        geo.tile0 = tile0;
 
         const uint32_t* in = p.src ? p.src : p.out;
         const uint32_t blocks = local_count >> R;
@@ -376,6 +376,109 @@ namespace hmpc_gb300
             if (gi != last)
             {
                 __syncthreads();
+            }
+        }
+    }
+
+    template<int L, int R, int Kind, int NW>
+    __global__ void __launch_bounds__(256, 2) ntt_pass_kernel(const NttPassParams p, const Modulus<L> m)
+    {
+        extern __shared__ uint32_t smem[];
+        ntt_process<L, R, Kind, NW>(p, m, static_cast<uint64_t>(blockIdx.x) << p.tile_bits, smem);
+    }
+
+    // ----------------------------------------------------------------------
+    // Persistent transform over a batch of polynomials of uneven degree.
+    // Work items are (pass of one polynomial, CTA tile group) in a list that
+    // holds every first-pass item before any later-pass item; CTAs take items
+    // in list order from an atomic counter.  An item of pass k of a
+    // polynomial waits until all earlier-pass items of that polynomial have
+    // signalled.  Every item it waits for was taken earlier by a running CTA
+    // that never waits on later items, so the waits end; they are still
+    // bounded, and a wait that runs out sets `error` and the kernel returns.
+    struct BatchedControl
+    {
+        uint32_t next;      // work counter
+        uint32_t error;     // nonzero: a wait ran out (value = item + 1)
+        uint32_t done;      // items finished
+        uint32_t pad;
+    };
+
+    struct BatchedParams
+    {
+        const NttPassParams* params;    // one per (polynomial, pass)
+        const uint32_t* item_param;     // item -> params index
+        const uint32_t* item_tile;      // item -> CTA tile group inside that pass
+        const uint32_t* item_wait;      // item -> signals needed before it may start (0: none)
+        const uint32_t* item_poly;      // item -> polynomial (counter index)
+        const uint32_t* item_signal;    // item -> 1 when it must signal its polynomial
+        uint32_t* counters;             // per polynomial
+        BatchedControl* control;
+        uint32_t items;
+        uint32_t spin_limit;            // polls of 64 ns before a wait gives up
+    };
+
+    __device__ __forceinline__ uint32_t load_acquire(const uint32_t* ptr)
+    {
+        uint32_t v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+        return v;
+    }
+
+    template<int L, int R>
+    __global__ void __launch_bounds__(256, 2) ntt_batched_kernel(const BatchedParams bp, const Modulus<L> m)
+    {
+        extern __shared__ uint32_t smem[];
+        __shared__ uint32_t item_s;
+        __shared__ uint32_t abort_s;
+        for (;;)
+        {
+            if (threadIdx.x == 0)
+            {
+                uint32_t item = atomicAdd(&bp.control->next, 1u);
+                uint32_t abort = 0;
+                if (item < bp.items)
+                {
+                    const uint32_t need = bp.item_wait[item];
+                    if (need)
+                    {
+                        const uint32_t* counter = bp.counters + bp.item_poly[item];
+                        uint32_t polls = 0;
+                        while (load_acquire(counter) < need)
+                        {
+                            if (++polls > bp.spin_limit || load_acquire(&bp.control->error))
+                            {
+                                atomicCAS(&bp.control->error, 0u, item + 1u);
+                                abort = 1;
+                                break;
+                            }
+                            __nanosleep(64);
+                        }
+                    }
+                }
+                item_s = item;
+                abort_s = abort;
+            }
+            __syncthreads();
+            const uint32_t item = item_s;
+            const uint32_t abort = abort_s;
+            __syncthreads();
+            if (item >= bp.items || abort)
+            {
+                return;
+            }
+            const NttPassParams& p = bp.params[bp.item_param[item]];
+            ntt_process<L, R, producer_tensor, 1>(p, m, static_cast<uint64_t>(bp.item_tile[item]) << p.tile_bits,
+                                                  smem);
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                if (bp.item_signal[item])
+                {
+                    __threadfence();
+                    atomicAdd(bp.counters + bp.item_poly[item], 1u);
+                }
+                atomicAdd(&bp.control->done, 1u);
             }
         }
     }

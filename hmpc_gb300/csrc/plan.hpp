@@ -23,6 +23,7 @@ namespace hmpc_gb300
         int max_local_bits = 0;   // 0: derived from the shared-memory budget
         int col_bits = 4;         // preferred coalescing width (2^c consecutive elements)
         int smem_budget = 112 * 1024;
+        bool spread_small_batches = true;  // shrink CTA tiles to fill the GPU when the batch is small
     };
 
     inline uint32_t smem_words(uint32_t local_count)
@@ -120,10 +121,15 @@ namespace hmpc_gb300
             const uint64_t tiles_per_poly = 1ull << (log_n - w - c);
             p.tiles = batch * tiles_per_poly;
             int tile_bits = std::max(0, b - w - c);
+            if (!o.spread_small_batches)
+            {
+                // whole CTA groups inside one polynomial
+                tile_bits = std::min(tile_bits, log_n - w - c);
+            }
             tile_bits = std::max(tile_bits, R - w - c);
             // keep at least ~2 CTAs per SM when the batch is small, as long as a
             // CTA still holds a full register block per thread
-            while (tile_bits > 0 && tile_bits + w + c > R + 5 &&
+            while (o.spread_small_batches && tile_bits > 0 && tile_bits + w + c > R + 5 &&
                    ((p.tiles + (1ull << tile_bits) - 1) >> tile_bits) < 304)
             {
                 --tile_bits;

@@ -51,6 +51,33 @@ def dec(queue, s, ct, p, plaintext_ntt=False, out=None):
     return out
 
 
+@dataclass
+class Ciphertext2:
+    """degree-2 ciphertext (c0, c1, c2): the product of two ciphertexts"""
+    c0: Tensor
+    c1: Tensor
+    c2: Tensor
+
+
+def mul(queue, x, y):
+    """ciphertext x ciphertext: the NTT-domain tensor product (no counterpart in
+    the reference, whose ciphertexts are linear only)"""
+    a0 = x.c0
+    out = Ciphertext2(*(make_tensor(a0.modulus, a0.shape, a0.n) for _ in range(3)))
+    _lib.call("hmpc_lhe_ct_mul", queue.handle, a0.modulus.handle, a0.elements, x.c0.ptr(), x.c1.ptr(), y.c0.ptr(),
+              y.c1.ptr(), out.c0.ptr(), out.c1.ptr(), out.c2.ptr())
+    return out
+
+
+def dec2(queue, s, ct, p, plaintext_ntt=False, out=None):
+    """decryption of a degree-2 ciphertext: c0 - s*c1 + s^2*c2"""
+    c0 = ct.c0
+    out = out or make_tensor(p, c0.shape, c0.n)
+    _lib.call("hmpc_lhe_dec2", queue.handle, c0.modulus.handle, p.handle, c0.n, c0.batch, s.ptr(), c0.ptr(),
+              ct.c1.ptr(), ct.c2.ptr(), int(plaintext_ntt), out.ptr())
+    return out
+
+
 def add(queue, x, y):
     """ciphertext + ciphertext (expr/crypto/lhe/ciphertext.hpp:49-53)"""
     return Ciphertext(queue.add(x.c0, y.c0), queue.add(x.c1, y.c1))

@@ -126,6 +126,39 @@ int hmpc_ntt_forward(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t 
 int hmpc_ntt_inverse(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const uint32_t* in,
                      uint32_t* out);
 
+/* The plain transform: one launch per stage over global memory, one thread
+ * per butterfly -- the schedule of the reference's SYCL kernels
+ * (number_theoretic_transform.hpp:90-197, 262-549) on this GPU; the comparator
+ * the tiled passes are measured against.  Same arguments and bit-identical
+ * results as hmpc_ntt_forward / hmpc_ntt_inverse. */
+int hmpc_ntt_forward_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch,
+                           const hmpc_producer* producer, uint32_t* out);
+int hmpc_ntt_inverse_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const uint32_t* in,
+                           uint32_t* out);
+
+/* --- batched transforms of uneven degree -------------------------------------
+ * A batch of polynomials of different degrees (powers of two >= 8), each in
+ * its own limb-planar buffer, transformed by ONE persistent kernel launch
+ * replayed from a captured CUDA graph.  The reference runs one transform per
+ * polynomial type (the degree is a template parameter, poly_mod.hpp:12-75).
+ * With autotune != 0 the register radix (4 or 8 elements per thread), the
+ * stages per shared-memory pass and the coalescing width are chosen by timing
+ * the candidates on the device at creation.  Same results as
+ * hmpc_ntt_forward / hmpc_ntt_inverse per polynomial. */
+typedef struct hmpc_ntt_batch hmpc_ntt_batch;
+int hmpc_ntt_batch_create(hmpc_context* ctx, hmpc_modulus* mod, uint64_t count, const uint64_t* degrees, int inverse,
+                          int autotune, hmpc_ntt_batch** out);
+/* in[i] / out[i]: degrees[i]*L words each (in[i] may equal out[i]); ordered
+ * on the context's stream. */
+int hmpc_ntt_batch_run(hmpc_ntt_batch* batch, const uint32_t* const* in, uint32_t* const* out);
+int hmpc_ntt_batch_info(const hmpc_ntt_batch* batch, int* radix_bits, int* local_bits, int* col_bits, uint32_t* items,
+                        float* tuned_ms);
+/* After a run: waits for it and reports whether every work item finished
+ * (HMPC_ERROR_TIMEOUT and the 1-based failing item when a bounded wait ran
+ * out). */
+int hmpc_ntt_batch_status(hmpc_ntt_batch* batch, uint32_t* failed_item);
+int hmpc_ntt_batch_destroy(hmpc_ntt_batch* batch);
+
 /* --- elementwise ----------------------------------------------------------- */
 /* d = a*b + c (examples/fma.cpp:56-67) */
 int hmpc_fma(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* a, const uint32_t* b,
@@ -186,6 +219,18 @@ int hmpc_lhe_enc_noalloc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, ui
  * -> cast to p (-> NTT_p when plaintext_ntt). */
 int hmpc_lhe_dec(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
                  const uint32_t* s, const uint32_t* c0, const uint32_t* c1, int plaintext_ntt, uint32_t* out);
+/* Decryption of a degree-2 ciphertext (c0, c1, c2), the result of
+ * hmpc_lhe_ct_mul: c0 - s*c1 + s^2*c2 -> INTT_q -> cast to p (-> NTT_p).  No
+ * counterpart in the reference. */
+int hmpc_lhe_dec2(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint64_t batch,
+                  const uint32_t* s, const uint32_t* c0, const uint32_t* c1, const uint32_t* c2, int plaintext_ntt,
+                  uint32_t* out);
+/* Ciphertext x ciphertext in NTT form: the tensor product
+ * (d0, d1, d2) = (a0*b0, a0*b1 + a1*b0, a1*b1) over `elements` residues.  No
+ * counterpart in the reference, whose ciphertexts are linear only
+ * (expr/crypto/lhe/ciphertext.hpp:49-81). */
+int hmpc_lhe_ct_mul(hmpc_context* ctx, hmpc_modulus* q, uint64_t elements, const uint32_t* a0, const uint32_t* a1,
+                    const uint32_t* b0, const uint32_t* b1, uint32_t* d0, uint32_t* d1, uint32_t* d2);
 /* Key generation; no counterpart in the reference, whose keys are plain
  * tensors (comp/crypto/lhe/key.hpp:7-12).  b <- uniform mod q (NTT form),
  * s <- NTT(CBD(1/2)), e <- NTT(CBD(10)), a = b*s + p*e, so that

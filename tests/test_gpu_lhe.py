@@ -92,3 +92,29 @@ def test_bgv_full_size_round_trip(queue):
     ct = lhe.enc(queue, key, msgs, gq)
     y = lhe.dec(queue, s, ct, gp)
     assert (y.data == msgs.data).all().item()
+
+
+def test_ciphertext_product_decrypts_to_plaintext_product(queue, oracle, cpu_threads):
+    """ct x ct (not in the reference): dec2(enc(m1) * enc(m2)) is the negacyclic
+    product m1*m2 mod p, and each product component matches the oracle."""
+    n, batch = 1 << 12, 2
+    om_q, om_p = oracle.Modulus(Q_256), oracle.Modulus(P_64)
+    gq, gp = queue.modulus(Q_256), queue.modulus(P_64)
+    queue.nonce = [7, 0, 0]
+    s, key = lhe.keygen(queue, gq, gp, n)
+    m1 = queue.uniform(gp, (batch,), n)
+    m2 = queue.uniform(gp, (batch,), n)
+    x = lhe.enc(queue, key, m1, gq)
+    y = lhe.enc(queue, key, m2, gq)
+    prod = lhe.mul(queue, x, y)
+    a0, a1, b0, b1 = (t.numpy() for t in (x.c0, x.c1, y.c0, y.c1))
+    mul = lambda u, v: oracle.binary(om_q, oracle.OP_MUL, u, v)  # noqa: E731
+    assert np.array_equal(prod.c0.numpy(), mul(a0, b0))
+    assert np.array_equal(prod.c1.numpy(), oracle.binary(om_q, oracle.OP_ADD, mul(a0, b1), mul(a1, b0)))
+    assert np.array_equal(prod.c2.numpy(), mul(a1, b1))
+    got = lhe.dec2(queue, s, prod, gp)
+    f1 = oracle.ntt(om_p, n, batch, src=m1.numpy(), threads=cpu_threads)
+    f2 = oracle.ntt(om_p, n, batch, src=m2.numpy(), threads=cpu_threads)
+    expect = oracle.ntt(om_p, n, batch, src=oracle.binary(om_p, oracle.OP_MUL, f1, f2), inverse=True,
+                        threads=cpu_threads)
+    assert np.array_equal(got.numpy(), expect)

@@ -186,3 +186,18 @@ def test_errors_are_reported(queue):
         queue.modulus(Q_FMA).prepare(8)  # not NTT friendly for N = 8 (Q = 1 mod 8 fails)
     with pytest.raises(_lib.HmpcError):
         queue.centered_binomial(gm, (4,), 65)
+
+
+@pytest.mark.parametrize("q,n,batch", [(Q_NTT, 4096, 1), (Q_256, 1 << 12, 2), (Q_192, 1 << 13, 1), (P_64, 16, 3)])
+def test_plain_transform_matches_tiled_and_oracle(queue, oracle, q, n, batch):
+    m = oracle.Modulus(q)
+    x = random_residues(oracle, m, n * batch, 21)
+    dx = upload(queue, q, x, (batch,), n)
+    y = queue.ntt_plain(dx)
+    assert np.array_equal(y.numpy(), oracle.ntt(m, n, batch, src=x))
+    assert np.array_equal(queue.ntt_plain(y, inverse=True).numpy(), x)
+    queue.nonce = [1, 2, 3]
+    a = queue.ntt_plain_centered_binomial(queue.modulus(q), n, (batch,), 20)
+    queue.nonce = [1, 2, 3]
+    b = queue.ntt_centered_binomial(queue.modulus(q), n, (batch,), 20)
+    assert np.array_equal(a.numpy(), b.numpy())
