@@ -113,6 +113,24 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(value, world, device=None):
+    """The slowest rank's time: every rank runs a full replica, so the job
+    finishes when the last one does (max reduction over the process group)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], device=device) if device is not None else torch.tensor([float(value)])
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, steps, elapsed_ms):
+    """units processed by all ranks per second of the slowest rank"""
+    return world * units_per_rank * steps / (elapsed_ms * 1e-3)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -252,6 +270,24 @@ def secondary_metrics(queue, int_peak):
         "tile": batch.info(),
     }
     batch.close()
+    del xs, ys
+
+    # serving: a seeded Poisson stream (mean 2000 requests/s) of transforms,
+    # encryptions and ciphertext products, N in 2^12..2^16, q of 4..8 limbs;
+    # continuous batching against plain per-request launches on the same stream
+    from hmpc_gb300.serving import Server, poisson_stream, prepare, replay
+
+    arrivals = poisson_stream(4000, rate=2000.0, seed=1)
+    p_mod, keys, shapes = prepare(queue, arrivals, slots=4)
+    serving = {"requests": len(arrivals), "offered_rate": 2000.0}
+    for mode, lanes, max_batch in (("continuous_batching", 4, 16), ("plain_per_request", 1, 1)):
+        server = Server(queue, memory_budget=4 << 30, lanes=lanes, max_batch=max_batch)
+        _, wall, st = replay(queue, server, arrivals, p_mod, keys, shapes)
+        server.close()
+        serving[mode] = {"throughput_req_s": st["completed"] / wall, "p50_ms": st["p50_us"] / 1e3,
+                         "p99_ms": st["p99_us"] / 1e3, "mean_batch": st["mean_batch"],
+                         "completed": st["completed"], "rejected": st["rejected"], "launches": st["launches"]}
+    out["serving_poisson_2000"] = serving
     return out
 
 
@@ -340,12 +376,8 @@ def main():
         stop.record(stream)
         barrier()
     launches = queue.launches - launches0
-    elapsed_ms = start.elapsed_time(stop)
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    value = world * BATCH * args.steps / (elapsed_ms * 1e-3)
+    elapsed_ms = max_over_ranks(start.elapsed_time(stop), world, device="cuda")
+    value = whole_job_rate(BATCH, world, args.steps, elapsed_ms)
 
     # ------------------------------------- e2e through the API, host buffers
     host_msgs = torch.empty(msgs.data.shape, dtype=torch.int32, pin_memory=True)
@@ -370,12 +402,8 @@ def main():
         e2e_step()
     e_stop.record(stream)
     barrier()
-    e2e_ms = e_start.elapsed_time(e_stop)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * BATCH * args.steps / (e2e_ms * 1e-3)
+    e2e_ms = max_over_ranks(e_start.elapsed_time(e_stop), world, device="cuda")
+    e2e_value = whole_job_rate(BATCH, world, args.steps, e2e_ms)
     # check the e2e result once: decrypting the copied-back ciphertext gives the messages
     back = lhe.Ciphertext(Tensor(q, (BATCH,), N, host_c0.to(queue.device)), Tensor(q, (BATCH,), N,
                                                                                host_c1.to(queue.device)))

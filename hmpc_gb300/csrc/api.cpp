@@ -77,7 +77,8 @@ namespace hmpc_gb300::detail
     }
 
     int run_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
-                      uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out)
+                      uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out, const uint32_t* poly_rng,
+                      uint32_t rng_slot)
     {
         if (int rc = enter(ctx))
         {
@@ -133,7 +134,7 @@ namespace hmpc_gb300::detail
             return fail(HMPC_ERROR_INVALID_ARGUMENT, "tensor producer without source");
         }
         const int log_n = __builtin_ctzll(n);
-        if (log_n < mod->kt->radix_bits)
+        if (log_n < mod->kt->radix_bits && !poly_rng)
         {
             // fewer stages than one register group holds: the per-stage kernel
             return run_plain(ctx, mod, n, batch, inverse, kind, vx2, security, src, out);
@@ -151,6 +152,8 @@ namespace hmpc_gb300::detail
             p.rng = rng;
             p.vx2 = vx2;
             p.top_mask = top_mask;
+            p.poly_rng = poly_rng;
+            p.rng_slot = rng_slot;
             const int k = i == 0 ? kind : producer_tensor;
             cudaError_t e = mod->kt->ntt_pass(p, k, k == producer_tensor ? 1 : nw, mod->h, plan[i].grid,
                                               plan[i].block, plan[i].smem, ctx->stream);
@@ -160,7 +163,7 @@ namespace hmpc_gb300::detail
             }
             ++ctx->launches;
         }
-        if (kind != producer_tensor)
+        if (kind != producer_tensor && !poly_rng)
         {
             nonce_add(ctx->nonce, n * batch);
         }

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -97,8 +98,11 @@ struct hmpc_modulus
         }
     }
 
+    std::mutex tables_mutex;  // the serving thread looks tables up while clients register new degrees
+
     int prepare(uint64_t n, hmpc_gb300::detail::Tables** out)
     {
+        std::lock_guard<std::mutex> lock(tables_mutex);
         auto it = tables.find(n);
         if (it == tables.end())
         {
@@ -135,7 +139,8 @@ namespace hmpc_gb300::detail
     int check_degree(uint64_t n);
     int enter(hmpc_context* ctx);
     int run_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
-                      uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
+                      uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out,
+                      const uint32_t* poly_rng = nullptr, uint32_t rng_slot = 0);
     int run_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                   uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
     CastParams make_cast(const hmpc_modulus* dst, const hmpc_modulus* src);

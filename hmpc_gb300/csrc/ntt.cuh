@@ -65,6 +65,12 @@ namespace hmpc_gb300
         RngKey rng;
         uint32_t vx2;                  // 2V for the CBD producer
         uint32_t top_mask;             // uniform producer: mask of the top word
+        // Per-polynomial RNG (batches of independent requests): when set,
+        // polynomial i draws with nonce = desc[0..2] + rng_slot * desc[4] * N and
+        // counter = desc[3] * N + coefficient, desc = poly_rng + 5 i -- exactly
+        // what the request would draw alone with its own nonce.
+        const uint32_t* poly_rng;
+        uint32_t rng_slot;
     };
 
     __device__ __forceinline__ uint32_t smem_addr(uint32_t local)
@@ -116,6 +122,26 @@ namespace hmpc_gb300
         }
     };
 
+    // generator key, nonce and counter of the stage-0 pair whose first element
+    // is coefficient idx_u of polynomial `poly`
+    __device__ __forceinline__ uint32_t pair_generator(const NttPassParams& p, uint64_t poly, uint64_t idx_u,
+                                                       RngKey& rng)
+    {
+        rng = p.rng;
+        if (p.poly_rng)
+        {
+            const uint32_t* d = p.poly_rng + poly * 5;
+            const uint64_t add = static_cast<uint64_t>(p.rng_slot) * d[4] << p.log_n;
+            uint64_t s = static_cast<uint64_t>(d[0]) + static_cast<uint32_t>(add);
+            rng.nonce[0] = static_cast<uint32_t>(s);
+            s = static_cast<uint64_t>(d[1]) + static_cast<uint32_t>(add >> 32) + (s >> 32);
+            rng.nonce[1] = static_cast<uint32_t>(s);
+            rng.nonce[2] = d[2] + static_cast<uint32_t>(s >> 32);
+            return static_cast<uint32_t>((static_cast<uint64_t>(d[3]) << p.log_n) + idx_u);
+        }
+        return static_cast<uint32_t>(poly * (1ull << p.log_n) + idx_u);
+    }
+
     template<int L, int Kind, int NW>
     __device__ __forceinline__ void produce_pair(const NttPassParams& p, const Modulus<L>& m, uint64_t poly,
                                                  uint64_t idx_u, uint64_t idx_v, uint32_t (&u)[L],
@@ -127,7 +153,9 @@ namespace hmpc_gb300
             // linear index; u draws first, v next (number_theoretic_transform.hpp
             // :316-329, comp/queue.hpp:191-212)
             uint32_t w[2 * NW];
-            chacha_stream<2 * NW>(p.rng, static_cast<uint32_t>(poly * (1ull << p.log_n) + idx_u), w);
+            RngKey rng;
+            const uint32_t counter = pair_generator(p, poly, idx_u, rng);
+            chacha_stream<2 * NW>(rng, counter, w);
             int a = 0, b = 0;
             const int count = 2 * static_cast<int>(p.vx2);
 #pragma unroll
@@ -147,7 +175,9 @@ namespace hmpc_gb300
         else if constexpr (Kind == producer_uniform)
         {
             uint32_t w[2 * NW];
-            chacha_stream<2 * NW>(p.rng, static_cast<uint32_t>(poly * (1ull << p.log_n) + idx_u), w);
+            RngKey rng;
+            const uint32_t counter = pair_generator(p, poly, idx_u, rng);
+            chacha_stream<2 * NW>(rng, counter, w);
             uniform_from_words<L, NW, 0, 2 * NW>(u, w, p.top_mask, m);
             uniform_from_words<L, NW, NW, 2 * NW>(v, w, p.top_mask, m);
         }

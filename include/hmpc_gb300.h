@@ -238,6 +238,74 @@ int hmpc_lhe_ct_mul(hmpc_context* ctx, hmpc_modulus* q, uint64_t elements, const
 int hmpc_lhe_keygen(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint32_t* s, uint32_t* a,
                     uint32_t* b);
 
+/* --- serving ---------------------------------------------------------------
+ * A request loop with continuous batching (no counterpart in the reference).
+ * Clients submit requests from any thread and get a ticket; a scheduler
+ * thread groups compatible pending requests (same kind, modulus, degree and
+ * key) into one dispatch per free lane (a device stream), so requests that
+ * arrive while others run are admitted as lanes and memory free up and their
+ * work overlaps on the device.  Scratch comes from a device pool reserved at
+ * creation (memory_budget_bytes): a dispatch waits until its scratch fits, a
+ * request that cannot fit even alone is rejected (HMPC_ERROR_REJECTED).  Keys
+ * and twiddle tables stay resident.  A request's result equals the result it
+ * has alone: an encryption draws its randomness from its own nonce with
+ * coefficient indices local to the request, exactly as hmpc_lhe_enc on a
+ * context whose nonce is the request's nonce. */
+typedef struct hmpc_server hmpc_server;
+typedef struct hmpc_server_config
+{
+    uint64_t memory_budget_bytes;    /* device pool for dispatch scratch */
+    uint32_t lanes;                  /* device streams, one dispatch each */
+    uint32_t max_batch;              /* requests per dispatch (1: no batching) */
+    uint32_t max_batch_polynomials;  /* polynomials per dispatch (0: 4096) */
+} hmpc_server_config;
+
+#define HMPC_REQUEST_NTT 0       /* out0 = NTT(in0): count polynomials of degree n mod q */
+#define HMPC_REQUEST_ENCRYPT 1   /* (out0, out1) = enc(key, in0): count plaintexts mod p, own nonce */
+#define HMPC_REQUEST_CT_MUL 2    /* (out0, out1, out2) = (in0, in1) x (in2, in3), count ciphertexts */
+typedef struct hmpc_request
+{
+    int kind;
+    uint32_t key_id;             /* HMPC_REQUEST_ENCRYPT: from hmpc_server_add_key */
+    hmpc_modulus* q;             /* NTT / CT_MUL modulus (ENCRYPT: the key's) */
+    uint64_t n;                  /* ring degree */
+    uint64_t count;              /* polynomials / plaintexts / ciphertexts */
+    const uint32_t* in0;
+    const uint32_t* in1;
+    const uint32_t* in2;
+    const uint32_t* in3;
+    uint32_t* out0;
+    uint32_t* out1;
+    uint32_t* out2;
+    uint32_t nonce[3];           /* HMPC_REQUEST_ENCRYPT: the request's RNG nonce */
+} hmpc_request;
+
+#define HMPC_REQUEST_QUEUED 0
+#define HMPC_REQUEST_RUNNING 1
+#define HMPC_REQUEST_DONE 2
+#define HMPC_REQUEST_FAILED (-2)
+
+typedef struct hmpc_server_stats
+{
+    uint64_t submitted, completed, rejected, failed, dispatches, launches;
+    double mean_batch;           /* requests per dispatch */
+    double p50_us, p99_us, mean_us;  /* submit -> completion observed, completed requests */
+} hmpc_server_stats;
+
+int hmpc_server_create(hmpc_context* ctx, const hmpc_server_config* config, hmpc_server** out);
+/* keep a public key (a, b: n words x L each, device memory) resident; the
+ * server copies it */
+int hmpc_server_add_key(hmpc_server* server, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, const uint32_t* a,
+                        const uint32_t* b, uint32_t* key_id);
+/* non-blocking; the buffers must stay valid until the request is done */
+int hmpc_server_submit(hmpc_server* server, const hmpc_request* request, uint64_t* ticket);
+/* state: HMPC_REQUEST_*; latency_us (may be NULL): submit -> completion */
+int hmpc_server_poll(hmpc_server* server, uint64_t ticket, int* state, double* latency_us);
+/* wait until every submitted request has finished */
+int hmpc_server_drain(hmpc_server* server, uint32_t timeout_ms);
+int hmpc_server_get_stats(hmpc_server* server, hmpc_server_stats* out);
+int hmpc_server_destroy(hmpc_server* server);
+
 #ifdef __cplusplus
 }
 #endif

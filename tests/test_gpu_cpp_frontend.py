@@ -36,6 +36,7 @@ def test_cpp_frontend(tmp_path, oracle):
     v = oracle.ntt(m, n, batch, sampler="cbd", variance_x2=20, key=KEY, nonce=[n * batch, 0, 0])
     assert np.array_equal(load("u.bin"), u)
     assert np.array_equal(load("v.bin"), v)
-    au = oracle.binary(m, oracle.OP_MUL, x[:, :n], u, elements=n * batch)
+    a = x.reshape(-1)[: n * m.limbs].reshape(m.limbs, n)  # the C++ test uploads the first n*L host words
+    au = oracle.binary(m, oracle.OP_MUL, a, u, elements=n * batch)
     w = oracle.ntt(m, n, batch, src=oracle.binary(m, oracle.OP_ADD, au, v), inverse=True)
     assert np.array_equal(load("w.bin"), w)
