@@ -236,15 +236,43 @@ def secondary_metrics(queue, int_peak):
     out["fma_2^24_L4"] = {"ms": ms, "GB/s": gbs, "hbm_frac": gbs / peak, "hbm_peak_source": source}
     del a, b, c, d
 
-    # single transform N = 4096, q 125-bit (examples/ntt.cpp modulus), batch 1
+    # single transform N = 4096, q 125-bit (examples/ntt.cpp modulus), batch 1:
+    # NTT then INTT, replayed from a CUDA graph so the device time is measured
+    # without host launch overhead (autotuned tile shape)
     qn = queue.modulus(MODULI["ntt"])
     qn.prepare(4096)
+    qn.tune(4096, 1)
+    qn.tune(4096, 1, inverse=True)
     x = queue.uniform(qn, (1,), 4096)
     y = Tensor(qn, (1,), 4096)
     z = Tensor(qn, (1,), 4096)
-    ms_tiled = time_ms(lambda: (queue.ntt(x, out=y), queue.intt(y, out=z)), 200)
-    ms_plain = time_ms(lambda: (queue.ntt_plain(x, out=y), queue.ntt_plain(y, out=z, inverse=True)), 200)
-    out["ntt_intt_4096_L4_batch1"] = {"us_tiled": ms_tiled * 1e3, "us_plain": ms_plain * 1e3}
+
+    def graphed(fn, reps=200):
+        side = torch.cuda.Stream()
+        queue.set_stream(side)
+        try:
+            with torch.cuda.stream(side):
+                fn()
+            side.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=side):
+                fn()
+            queue.set_stream(stream)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(side)
+            for _ in range(reps):
+                g.replay()
+            b.record(side)
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+        finally:
+            queue.set_stream(stream)
+
+    us_tiled = graphed(lambda: (queue.ntt(x, out=y), queue.intt(y, out=z))) * 1e3
+    us_plain = graphed(lambda: (queue.ntt_plain(x, out=y), queue.ntt_plain(y, out=z, inverse=True))) * 1e3
+    out["ntt_intt_4096_L4_batch1"] = {"us_tiled_graph": us_tiled, "us_plain_graph": us_plain,
+                                      "round_trip_ok": bool((z.data == x.data).all().item())}
 
     # batched uneven degrees: one persistent graph launch vs one plain call per polynomial
     degrees = uneven_degrees(512)
@@ -277,17 +305,19 @@ def secondary_metrics(queue, int_peak):
     # continuous batching against plain per-request launches on the same stream
     from hmpc_gb300.serving import Server, poisson_stream, prepare, replay
 
-    arrivals = poisson_stream(4000, rate=2000.0, seed=1)
-    p_mod, keys, shapes = prepare(queue, arrivals, slots=4)
-    serving = {"requests": len(arrivals), "offered_rate": 2000.0}
-    for mode, lanes, max_batch in (("continuous_batching", 4, 16), ("plain_per_request", 1, 1)):
-        server = Server(queue, memory_budget=4 << 30, lanes=lanes, max_batch=max_batch)
-        _, wall, st = replay(queue, server, arrivals, p_mod, keys, shapes)
-        server.close()
-        serving[mode] = {"throughput_req_s": st["completed"] / wall, "p50_ms": st["p50_us"] / 1e3,
-                         "p99_ms": st["p99_us"] / 1e3, "mean_batch": st["mean_batch"],
-                         "completed": st["completed"], "rejected": st["rejected"], "launches": st["launches"]}
-    out["serving_poisson_2000"] = serving
+    for rate in (2000.0, 10000.0):
+        arrivals = poisson_stream(4000, rate=rate, seed=1)
+        p_mod, keys, shapes = prepare(queue, arrivals, slots=4)
+        serving = {"requests": len(arrivals), "offered_rate": rate}
+        for mode, lanes, max_batch in (("continuous_batching", 4, 16), ("plain_per_request", 1, 1)):
+            server = Server(queue, memory_budget=4 << 30, lanes=lanes, max_batch=max_batch)
+            _, wall, st = replay(queue, server, arrivals, p_mod, keys, shapes)
+            server.close()
+            serving[mode] = {"throughput_req_s": st["completed"] / wall, "p50_ms": st["p50_us"] / 1e3,
+                             "p99_ms": st["p99_us"] / 1e3, "mean_batch": st["mean_batch"],
+                             "completed": st["completed"], "rejected": st["rejected"], "launches": st["launches"]}
+        out[f"serving_poisson_{int(rate)}"] = serving
+        del shapes, keys
     return out
 
 
@@ -348,6 +378,8 @@ def main():
     q, p = queue.modulus(Q_256), queue.modulus(P_64)
     q.prepare(N)
     p.prepare(N)
+    # autotune the tile shape of the batch's transforms (kept per modulus)
+    q.tune(N, BATCH)
     queue.nonce = [0, 0, 0]
     s0, key0 = lhe.keygen(queue, q, p, N)
     msgs = queue.uniform(p, (BATCH,), N)

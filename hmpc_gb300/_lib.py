@@ -61,6 +61,8 @@ SIGNATURES = {
     "hmpc_modulus_info": ([_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), _u32p], _int),
     "hmpc_modulus_prepare": ([_vp, _u64], _int),
     "hmpc_modulus_root": ([_vp, _u64, _int, _u32p], _int),
+    "hmpc_modulus_set_plan": ([_vp, _u64, _u64, _int, _int, _int, _int], _int),
+    "hmpc_modulus_tune": ([_vp, _u64, _u64, _int, ctypes.POINTER(ctypes.c_float)], _int),
     "hmpc_modulus_twiddles": ([_vp, _u64, _int, _u32p], _int),
     "hmpc_tensor_alloc": ([_vp, _u64, ctypes.POINTER(_vp)], _int),
     "hmpc_tensor_free": ([_vp, _vp], _int),

@@ -51,6 +51,15 @@ class Modulus:
     def prepare(self, n):
         _lib.call("hmpc_modulus_prepare", self.handle, n)
 
+    def set_plan(self, n, batch, inverse=False, radix_bits=3, local_bits=0, col_bits=4):
+        _lib.call("hmpc_modulus_set_plan", self.handle, n, batch, int(inverse), radix_bits, local_bits, col_bits)
+
+    def tune(self, n, batch, inverse=False):
+        """time the tile shapes for this (degree, batch, direction); returns ms"""
+        ms = ctypes.c_float()
+        _lib.call("hmpc_modulus_tune", self.handle, n, batch, int(inverse), ctypes.byref(ms))
+        return ms.value
+
     def root(self, n, inverse=False):
         out = (ctypes.c_uint32 * 16)()
         _lib.call("hmpc_modulus_root", self.handle, n, int(inverse), out)

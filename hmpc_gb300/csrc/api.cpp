@@ -139,7 +139,19 @@ namespace hmpc_gb300::detail
             // fewer stages than one register group holds: the per-stage kernel
             return run_plain(ctx, mod, n, batch, inverse, kind, vx2, security, src, out);
         }
-        const std::vector<PassPlan> plan = plan_transform(L, log_n, batch, inverse, mod->kt->radix_bits);
+        hmpc_modulus::TileChoice choice;
+        {
+            std::lock_guard<std::mutex> lock(mod->tables_mutex);
+            auto it = mod->tile_choices.find(std::make_tuple(log_n, inverse ? 1 : 0, batch));
+            if (it != mod->tile_choices.end())
+            {
+                choice = it->second;
+            }
+        }
+        PlanOptions options;
+        options.max_local_bits = choice.local_bits;
+        options.col_bits = choice.col_bits;
+        const std::vector<PassPlan> plan = plan_transform(L, log_n, batch, inverse, choice.radix_bits, options);
         const RngKey rng = ctx->rng();
         for (size_t i = 0; i < plan.size(); ++i)
         {
@@ -155,7 +167,8 @@ namespace hmpc_gb300::detail
             p.poly_rng = poly_rng;
             p.rng_slot = rng_slot;
             const int k = i == 0 ? kind : producer_tensor;
-            cudaError_t e = mod->kt->ntt_pass(p, k, k == producer_tensor ? 1 : nw, mod->h, plan[i].grid,
+            cudaError_t e = mod->kt->ntt_pass(p, k, k == producer_tensor ? 1 : nw, choice.radix_bits, mod->h,
+                                              plan[i].grid,
                                               plan[i].block, plan[i].smem, ctx->stream);
             if (e != cudaSuccess)
             {
@@ -571,6 +584,122 @@ int hmpc_modulus_prepare(hmpc_modulus* mod, uint64_t n)
         return rc;
     }
     return mod->prepare(n, nullptr);
+}
+
+int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits,
+                          int local_bits, int col_bits)
+{
+    if (!mod)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    if ((radix_bits != 2 && radix_bits != 3) || local_bits < 0 || local_bits > 13 || col_bits < 0 || col_bits > 6 ||
+        (local_bits && static_cast<uint64_t>(mod->c.limbs) * 4u * smem_words(1u << local_bits) > 200 * 1024))
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "tile shape out of range");
+    }
+    std::lock_guard<std::mutex> lock(mod->tables_mutex);
+    mod->tile_choices[std::make_tuple(__builtin_ctzll(n), inverse ? 1 : 0, batch)] = {radix_bits, local_bits,
+                                                                                      col_bits};
+    return HMPC_OK;
+}
+
+int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, float* best_ms)
+{
+    if (!mod)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
+    }
+    hmpc_context* ctx = mod->ctx;
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    if (batch == 0)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "empty batch");
+    }
+    if (int rc = mod->prepare(n, nullptr))
+    {
+        return rc;
+    }
+    const int L = mod->c.limbs;
+    const uint64_t words = n * batch * static_cast<uint64_t>(L);
+    uint32_t* buf = nullptr;
+    if (cudaMalloc(&buf, words * sizeof(uint32_t)) != cudaSuccess)
+    {
+        return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tuning scratch");
+    }
+    cudaMemsetAsync(buf, 0, words * sizeof(uint32_t), ctx->stream);
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    const int log_n = __builtin_ctzll(n);
+    const auto key = std::make_tuple(log_n, inverse ? 1 : 0, batch);
+    PlanOptions def;
+    const int b0 = local_bits_for(L, def);
+    float best = 1e30f;
+    hmpc_modulus::TileChoice best_choice;
+    for (int R : {3, 2})
+    {
+        for (int lb = std::max(R + 2, b0 - 5); lb <= std::min(13, b0 + 1); ++lb)
+        {
+            if (static_cast<uint64_t>(L) * 4u * smem_words(1u << lb) > 200 * 1024)
+            {
+                continue;
+            }
+            for (int c : {3, 4, 5})
+            {
+                {
+                    std::lock_guard<std::mutex> lock(mod->tables_mutex);
+                    mod->tile_choices[key] = {R, lb, c};
+                }
+                float sample = 1e30f;
+                for (int rep = 0; rep < 4; ++rep)
+                {
+                    cudaEventRecord(t0, ctx->stream);
+                    if (run_transform(ctx, mod, n, batch, inverse, producer_tensor, 0, 0, buf, buf) != HMPC_OK)
+                    {
+                        sample = 1e30f;
+                        break;
+                    }
+                    cudaEventRecord(t1, ctx->stream);
+                    cudaEventSynchronize(t1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, t0, t1);
+                    if (rep)
+                    {
+                        sample = std::min(sample, ms);
+                    }
+                }
+                if (sample < best)
+                {
+                    best = sample;
+                    best_choice = {R, lb, c};
+                }
+            }
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lock(mod->tables_mutex);
+        mod->tile_choices[key] = best_choice;
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaFree(buf);
+    if (best_ms)
+    {
+        *best_ms = best;
+    }
+    return HMPC_OK;
 }
 
 int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root)

@@ -43,8 +43,8 @@ namespace hmpc_gb300
 
     struct KernelTable
     {
-        cudaError_t (*ntt_pass)(const NttPassParams& p, int kind, int nw, const HostModulus& m, unsigned grid,
-                                unsigned block, size_t smem, cudaStream_t stream);
+        cudaError_t (*ntt_pass)(const NttPassParams& p, int kind, int nw, int radix_bits, const HostModulus& m,
+                                unsigned grid, unsigned block, size_t smem, cudaStream_t stream);
         cudaError_t (*fma)(uint32_t* d, const uint32_t* a, const uint32_t* b, const uint32_t* c, uint64_t elements,
                            const HostModulus& m, cudaStream_t stream);
         cudaError_t (*binary)(uint32_t* out, const uint32_t* a, uint64_t a_elements, const uint32_t* b,

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -98,6 +99,15 @@ struct hmpc_modulus
         }
     }
 
+    // tile shape per (log2 N, inverse, batch): register radix bits, tile
+    // bits, column bits -- set by hmpc_modulus_tune / hmpc_modulus_set_plan
+    struct TileChoice
+    {
+        int radix_bits = 3;
+        int local_bits = 0;
+        int col_bits = 4;
+    };
+    std::map<std::tuple<int, int, uint64_t>, TileChoice> tile_choices;
     std::mutex tables_mutex;  // the serving thread looks tables up while clients register new degrees
 
     int prepare(uint64_t n, hmpc_gb300::detail::Tables** out)

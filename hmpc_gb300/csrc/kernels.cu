@@ -50,11 +50,11 @@ namespace hmpc_gb300
             return static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(g, 152ull * 64ull)));
         }
 
-        template<int Kind, int NW>
+        template<int Kind, int NW, int RB>
         cudaError_t launch_pass(const NttPassParams& p, const Modulus<L>& m, unsigned grid, unsigned block,
                                 size_t smem, cudaStream_t stream)
         {
-            auto kernel = ntt_pass_kernel<L, R, Kind, NW>;
+            auto kernel = ntt_pass_kernel<L, RB, Kind, NW>;
             static bool configured = false;
             if (!configured)
             {
@@ -69,22 +69,22 @@ namespace hmpc_gb300
             return cudaGetLastError();
         }
 
-        cudaError_t ntt_pass(const NttPassParams& p, int kind, int nw, const HostModulus& h, unsigned grid,
-                             unsigned block, size_t smem, cudaStream_t stream)
+        template<int RB>
+        cudaError_t ntt_pass_radix(const NttPassParams& p, int kind, int nw, const Modulus<L>& m, unsigned grid,
+                                   unsigned block, size_t smem, cudaStream_t stream)
         {
-            const Modulus<L> m = device_modulus(h);
             if (kind == producer_tensor)
             {
-                return launch_pass<producer_tensor, 1>(p, m, grid, block, smem, stream);
+                return launch_pass<producer_tensor, 1, RB>(p, m, grid, block, smem, stream);
             }
             if (kind == producer_cbd)
             {
                 switch (nw)
                 {
-                case 1: return launch_pass<producer_cbd, 1>(p, m, grid, block, smem, stream);
-                case 2: return launch_pass<producer_cbd, 2>(p, m, grid, block, smem, stream);
-                case 3: return launch_pass<producer_cbd, 3>(p, m, grid, block, smem, stream);
-                case 4: return launch_pass<producer_cbd, 4>(p, m, grid, block, smem, stream);
+                case 1: return launch_pass<producer_cbd, 1, RB>(p, m, grid, block, smem, stream);
+                case 2: return launch_pass<producer_cbd, 2, RB>(p, m, grid, block, smem, stream);
+                case 3: return launch_pass<producer_cbd, 3, RB>(p, m, grid, block, smem, stream);
+                case 4: return launch_pass<producer_cbd, 4, RB>(p, m, grid, block, smem, stream);
                 default: return cudaErrorInvalidValue;
                 }
             }
@@ -92,12 +92,27 @@ namespace hmpc_gb300
             {
                 if (nw == L + 2)
                 {
-                    return launch_pass<producer_uniform, L + 2>(p, m, grid, block, smem, stream);
+                    return launch_pass<producer_uniform, L + 2, RB>(p, m, grid, block, smem, stream);
                 }
                 if (nw == L + 3)
                 {
-                    return launch_pass<producer_uniform, L + 3>(p, m, grid, block, smem, stream);
+                    return launch_pass<producer_uniform, L + 3, RB>(p, m, grid, block, smem, stream);
                 }
+            }
+            return cudaErrorInvalidValue;
+        }
+
+        cudaError_t ntt_pass(const NttPassParams& p, int kind, int nw, int radix_bits, const HostModulus& h,
+                             unsigned grid, unsigned block, size_t smem, cudaStream_t stream)
+        {
+            const Modulus<L> m = device_modulus(h);
+            if (radix_bits == 2)
+            {
+                return ntt_pass_radix<2>(p, kind, nw, m, grid, block, smem, stream);
+            }
+            if (radix_bits == 3)
+            {
+                return ntt_pass_radix<3>(p, kind, nw, m, grid, block, smem, stream);
             }
             return cudaErrorInvalidValue;
         }

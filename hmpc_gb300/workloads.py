@@ -73,12 +73,20 @@ def main(argv=None):
     ap.add_argument("--vx2", type=int, default=20)
     ap.add_argument("--elements", type=int, default=1 << 24)
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--tune", action="store_true", help="autotune the tile shape first")
+    ap.add_argument("--radix-bits", type=int, default=0, help="force a tile shape (with --local-bits, --col-bits)")
+    ap.add_argument("--local-bits", type=int, default=0)
+    ap.add_argument("--col-bits", type=int, default=4)
     args = ap.parse_args(argv)
     queue = Queue(key=KEY)
     q = queue.modulus(MODULI[args.q])
     result = {"workload": args.workload, "q_limbs": q.limbs}
     if args.workload in ("ntt", "intt", "ntt-cbd", "ntt-uniform", "plain-ntt"):
         q.prepare(args.n)
+        if args.tune:
+            result["tuned_ms"] = q.tune(args.n, args.batch, inverse=args.workload == "intt")
+        elif args.radix_bits:
+            q.set_plan(args.n, args.batch, args.workload == "intt", args.radix_bits, args.local_bits, args.col_bits)
         x = queue.uniform(q, (args.batch,), args.n)
         out = Tensor(q, (args.batch,), args.n)
         if args.workload == "ntt":

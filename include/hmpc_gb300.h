@@ -89,6 +89,15 @@ int hmpc_modulus_prepare(hmpc_modulus* mod, uint64_t n);
 /* psi (inverse = 0) or psi^-1 (inverse = 1) for degree n, Montgomery form,
  * L words (hmpc/ints/num/theory/root_of_unity.hpp:20-54). */
 int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root);
+/* Tile shape of the transforms of degree n over `batch` polynomials in one
+ * direction: register radix bits (2 or 3: 4 or 8 elements per thread), tile
+ * bits (log2 elements a CTA stages; 0 = by shared-memory budget) and column
+ * bits (coalescing width).  No counterpart in the reference (its transform
+ * has one schedule).  hmpc_modulus_tune times the candidates on the device
+ * (scratch buffers, values irrelevant to the cost) and keeps the fastest. */
+int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits, int local_bits,
+                          int col_bits);
+int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, float* best_ms);
 /* Copy a cached twiddle table (n*L words, element-major) to host memory. */
 int hmpc_modulus_twiddles(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* host_table);
 

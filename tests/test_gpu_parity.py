@@ -201,3 +201,34 @@ def test_plain_transform_matches_tiled_and_oracle(queue, oracle, q, n, batch):
     queue.nonce = [1, 2, 3]
     b = queue.ntt_centered_binomial(queue.modulus(q), n, (batch,), 20)
     assert np.array_equal(a.numpy(), b.numpy())
+
+
+@pytest.mark.parametrize("radix_bits,local_bits,col_bits", [(2, 0, 4), (2, 8, 3), (3, 9, 5), (2, 11, 5), (3, 6, 3)])
+@pytest.mark.parametrize("q,n,batch", [(Q_256, 1 << 15, 2), (Q_192, 1 << 12, 3), (P_64, 1 << 16, 1),
+                                       (Q_NTT, 1 << 13, 2)])
+def test_tile_shapes_give_identical_transforms(queue, oracle, q, n, batch, radix_bits, local_bits, col_bits,
+                                               cpu_threads):
+    m = oracle.Modulus(q)
+    gm = queue.modulus(q)
+    x = random_residues(oracle, m, n * batch, 33)
+    for inverse in (False, True):
+        gm.set_plan(n, batch, inverse, radix_bits, local_bits, col_bits)
+    ref = oracle.ntt(m, n, batch, src=x, threads=cpu_threads)
+    y = queue.ntt(upload(queue, q, x, (batch,), n))
+    assert np.array_equal(y.numpy(), ref)
+    assert np.array_equal(queue.intt(y).numpy(), x)
+    queue.nonce = [9, 9, 9]
+    c = queue.ntt_centered_binomial(gm, n, (batch,), 20)
+    assert np.array_equal(c.numpy(), oracle.ntt(m, n, batch, sampler="cbd", variance_x2=20, key=KEY,
+                                                nonce=[9, 9, 9], threads=cpu_threads))
+    for inverse in (False, True):
+        gm.set_plan(n, batch, inverse, 3, 0, 4)  # back to the default shape
+
+
+def test_tuner_keeps_results_identical(queue, oracle):
+    m = oracle.Modulus(Q_256)
+    gm = queue.modulus(Q_256)
+    n, batch = 1 << 12, 8
+    x = random_residues(oracle, m, n * batch, 44)
+    assert gm.tune(n, batch) > 0
+    assert np.array_equal(queue.ntt(upload(queue, Q_256, x, (batch,), n)).numpy(), oracle.ntt(m, n, batch, src=x))
