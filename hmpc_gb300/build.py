@@ -55,7 +55,7 @@ def build(verbose=False, jobs=None):
         objects.append(obj)
         if _stale(obj, [CSRC / "kernels.cu", *headers]):
             steps.append(common + [f"-DHMPC_L={limbs}", "-c", str(CSRC / "kernels.cu"), "-o", str(obj)])
-    for name in ("api.cpp", "host_math.cpp", "probe.cu", "noalloc.cu", "batched.cpp", "serve.cpp"):
+    for name in ("api.cpp", "host_math.cpp", "probe.cu", "noalloc.cu", "batched.cpp", "serve.cpp", "cipher.cu"):
         obj = OUT / (name.rsplit(".", 1)[0] + ".o")
         objects.append(obj)
         if _stale(obj, [CSRC / name, *headers]):

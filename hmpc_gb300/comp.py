@@ -263,6 +263,21 @@ class Queue:
         _lib.call("hmpc_cast", self.handle, modulus.handle, x.modulus.handle, x.elements, x.ptr(), out.ptr())
         return out
 
+    def cipher_enc(self, key, nonce, x):
+        """enc(cipher(key, nonce), tensor(x)): element-major int32 words
+        (expr/crypto/cipher.hpp:59-173)"""
+        out = torch.empty(x.elements * x.modulus.limbs, dtype=torch.int32, device=self.device)
+        _lib.call("hmpc_cipher_enc", self.handle, _u32_array(key), _u32_array(nonce), x.elements, x.modulus.limbs,
+                  x.ptr(), _ptr(out))
+        return out
+
+    def cipher_dec(self, key, nonce, words, modulus, shape, n=1):
+        """dec<T>(cipher(key, nonce), y) back to a limb-planar tensor"""
+        out = make_tensor(modulus, shape, n)
+        _lib.call("hmpc_cipher_dec", self.handle, _u32_array(key), _u32_array(nonce), out.elements, modulus.limbs,
+                  _ptr(words), out.ptr())
+        return out
+
     def to_montgomery(self, x, out=None):
         out = out or make_tensor(x.modulus, x.shape, x.n)
         _lib.call("hmpc_to_montgomery", self.handle, x.modulus.handle, x.elements, x.ptr(), out.ptr())

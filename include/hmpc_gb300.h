@@ -247,6 +247,18 @@ int hmpc_lhe_ct_mul(hmpc_context* ctx, hmpc_modulus* q, uint64_t elements, const
 int hmpc_lhe_keygen(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n, uint32_t* s, uint32_t* a,
                     uint32_t* b);
 
+/* --- stream cipher -----------------------------------------------------------
+ * enc(cipher(key, nonce), x) / dec<T>(cipher(key, nonce), y) of
+ * hmpc/expr/crypto/cipher.hpp:59-319: element i's `limbs` words are XORed with
+ * keystream words i*limbs .. i*limbs+limbs-1 of ChaCha20(key, nonce, counter
+ * from 0).  enc reads a limb-planar tensor and writes the reference's
+ * element-major limb tensor (flat_out[i*limbs + j]); dec is the reverse.
+ * Independent of the context's RNG capability (explicit key and nonce). */
+int hmpc_cipher_enc(hmpc_context* ctx, const uint32_t key[8], const uint32_t nonce[3], uint64_t elements, int limbs,
+                    const uint32_t* planar_in, uint32_t* flat_out);
+int hmpc_cipher_dec(hmpc_context* ctx, const uint32_t key[8], const uint32_t nonce[3], uint64_t elements, int limbs,
+                    const uint32_t* flat_in, uint32_t* planar_out);
+
 /* --- serving ---------------------------------------------------------------
  * A request loop with continuous batching (no counterpart in the reference).
  * Clients submit requests from any thread and get a ticket; a scheduler

@@ -1155,3 +1155,67 @@ int orc_lhe_keygen(const orc_modulus* q, const orc_modulus* p, uint64_t n, const
     free(e);
     return rc;
 }
+
+/* ---------------------------------------------------------------- cipher -- */
+
+/* expr/crypto/cipher.hpp:128-173: the work is cut into batches of
+ * lcm(16, limbs) words; batch b starts a generator at counter
+ * b * (batch / 16) and consumes one word per limb of its elements in order --
+ * so word w of the element-major output uses word w % 16 of block w / 16. */
+static uint64_t gcd_u64(uint64_t a, uint64_t b)
+{
+    while (b)
+    {
+        uint64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+static void cipher_batches(const uint32_t key[8], const uint32_t nonce[3], uint64_t elements, int limbs,
+                           const uint32_t* in, uint32_t* out, int decrypt)
+{
+    const uint64_t batch = 16 / gcd_u64(16, (uint64_t)limbs) * (uint64_t)limbs;
+    const uint64_t per_batch = batch / (uint64_t)limbs;
+    const uint64_t blocks = batch / 16;
+    const uint64_t count = (elements * (uint64_t)limbs + batch - 1) / batch;
+#pragma omp parallel for schedule(static)
+    for (int64_t b = 0; b < (int64_t)count; ++b)
+    {
+        orc_generator g;
+        orc_generator_init(&g, key, nonce, (uint32_t)((uint64_t)b * blocks));
+        for (uint64_t e = 0; e < per_batch; ++e)
+        {
+            uint64_t i = (uint64_t)b * per_batch + e;
+            if (i >= elements)
+            {
+                break;
+            }
+            for (int j = 0; j < limbs; ++j)
+            {
+                uint32_t mask = orc_generator_next(&g);
+                if (!decrypt)
+                {
+                    out[i * (uint64_t)limbs + (uint64_t)j] = in[(uint64_t)j * elements + i] ^ mask;
+                }
+                else
+                {
+                    out[(uint64_t)j * elements + i] = in[i * (uint64_t)limbs + (uint64_t)j] ^ mask;
+                }
+            }
+        }
+    }
+}
+
+void orc_cipher_enc(const uint32_t key[8], const uint32_t nonce[3], uint64_t elements, int limbs,
+                    const uint32_t* planar_in, uint32_t* flat_out)
+{
+    cipher_batches(key, nonce, elements, limbs, planar_in, flat_out, 0);
+}
+
+void orc_cipher_dec(const uint32_t key[8], const uint32_t nonce[3], uint64_t elements, int limbs,
+                    const uint32_t* flat_in, uint32_t* planar_out)
+{
+    cipher_batches(key, nonce, elements, limbs, flat_in, planar_out, 1);
+}

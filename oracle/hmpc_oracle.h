@@ -160,6 +160,16 @@ int orc_lhe_dec(const orc_modulus* q, const orc_modulus* p, uint64_t n, uint64_t
 int orc_lhe_keygen(const orc_modulus* q, const orc_modulus* p, uint64_t n, const uint32_t key[8], uint32_t nonce[3],
                    uint32_t* s, uint32_t* a, uint32_t* b, int threads);
 
+/* ChaCha20 stream cipher over a tensor (expr/crypto/cipher.hpp:59-173,
+ * crypto/cipher.hpp:29-44): element i's limbs (limb-planar input, `limbs`
+ * words each) are XORed with keystream words i*limbs .. i*limbs+limbs-1 of
+ * ChaCha20(key, nonce, counter from 0) and written element-major
+ * (out[i*limbs + j]).  dec reads element-major and writes limb-planar. */
+void orc_cipher_enc(const uint32_t key[8], const uint32_t nonce[3], uint64_t elements, int limbs,
+                    const uint32_t* planar_in, uint32_t* flat_out);
+void orc_cipher_dec(const uint32_t key[8], const uint32_t nonce[3], uint64_t elements, int limbs,
+                    const uint32_t* flat_in, uint32_t* planar_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -362,5 +362,21 @@ def lhe_dec(q, p, n, batch, s, c0, c1, plaintext_ntt, threads=0):
     return out
 
 
+def cipher_enc(key, nonce, planar):
+    planar = np.ascontiguousarray(planar, dtype=np.uint32)
+    limbs, elements = planar.shape
+    out = np.zeros(limbs * elements, dtype=np.uint32)
+    lib().orc_cipher_enc(_u32(key), _u32(nonce), ctypes.c_uint64(elements), limbs, _ptr(planar), _ptr(out))
+    return out
+
+
+def cipher_dec(key, nonce, flat, limbs):
+    flat = np.ascontiguousarray(flat, dtype=np.uint32)
+    elements = flat.size // limbs
+    out = np.zeros((limbs, elements), dtype=np.uint32)
+    lib().orc_cipher_dec(_u32(key), _u32(nonce), ctypes.c_uint64(elements), limbs, _ptr(flat), _ptr(out))
+    return out
+
+
 def cpu_threads():
     return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()

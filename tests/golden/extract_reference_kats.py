@@ -88,6 +88,27 @@ def chacha_vectors(root):
     return out
 
 
+def cipher_vectors(root):
+    rel = "tests/crypto/cipher.cpp"
+    text = (root / rel).read_text()
+
+    def array(name):
+        m = re.search(r"hmpc::core::uint(?:8|32) const " + name + r"\[\] =\s*\{([^}]*)\}", text)
+        return [h(x.strip()) for x in m.group(1).replace("\n", " ").split(",") if x.strip()]
+
+    start = text.index("plaintext_bytes[]")
+    line = text[:start].count("\n") + 1
+    return {
+        "file": rel,
+        "key": array("key"),
+        "nonce": array("nonce"),
+        "counter": array("counter")[0],
+        "plaintext": array("plaintext_bytes"),
+        "ciphertext": array("expected_ciphertext_bytes"),
+        "lines": f"{rel}:{line}",
+    }
+
+
 def mod_vectors(root):
     rel = "tests/ints/mod.cpp"
     src = lines_of(root / rel)
@@ -166,6 +187,7 @@ def main():
     data = {
         "source": "hmpc v0.5.2 Catch2 tests, read as text",
         "chacha20": chacha_vectors(root),
+        "cipher": cipher_vectors(root),
         "mod": mod_vectors(root),
         "poly_mod_ntt": poly_mod_vectors(root),
         "root_of_unity": root_of_unity_vectors(root),

@@ -239,3 +239,37 @@ def test_lhe_keygen_enc_dec_small(oracle):
     c0, c1, _ = oracle.lhe_enc(q, p, n, batch, a, b, msgs, False, key, oracle.nonce_add(nonce, n * batch))
     y = oracle.lhe_dec(q, p, n, batch, s, c0, c1, False)
     assert np.array_equal(y, msgs)
+
+
+def _words_le(byts):
+    padded = list(byts) + [0] * (-len(byts) % 4)
+    return [padded[i] | padded[i + 1] << 8 | padded[i + 2] << 16 | padded[i + 3] << 24 for i in range(0, len(padded), 4)]
+
+
+def test_cipher_rfc8439_vector(oracle, kats):
+    """RFC 8439 section 2.4.2 (tests/crypto/cipher.cpp): the keystream starts at
+    block counter 1, so a zero block is put in front of the message."""
+    c = kats["cipher"]
+    msg = _words_le(c["plaintext"])
+    planar = np.array([[0] * 16 + msg], dtype=np.uint32)
+    out = oracle.cipher_enc(c["key"], c["nonce"], planar)
+    got = b"".join(int(w).to_bytes(4, "little") for w in out[16:])[: len(c["ciphertext"])]
+    assert list(got) == c["ciphertext"]
+    back = oracle.cipher_dec(c["key"], c["nonce"], out, 1)
+    assert np.array_equal(back, planar)
+
+
+@pytest.mark.parametrize("limbs", [1, 3, 4, 5, 8, 16])
+def test_cipher_batches_equal_plain_keystream(oracle, limbs):
+    """the reference's lcm(16, L)-word batches are the plain keystream"""
+    key, nonce = [42] + [0] * 7, [1, 0, 0]
+    elements = 37
+    rng = np.random.default_rng(limbs)
+    planar = rng.integers(0, 2**32, size=(limbs, elements), dtype=np.uint64).astype(np.uint32)
+    out = oracle.cipher_enc(key, nonce, planar)
+    words = elements * limbs
+    stream = []
+    for blk in range((words + 15) // 16):
+        stream += py.chacha20_block(key, blk, nonce)
+    flat = planar.T.reshape(-1)
+    assert np.array_equal(out, flat ^ np.array(stream[:words], dtype=np.uint32))
