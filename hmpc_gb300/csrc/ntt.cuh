@@ -413,7 +413,7 @@ namespace hmpc_gb300
     // R = 3 (8 elements per thread) fits 2 CTAs of 256 threads per SM at
     // L = 8; R = 2 (4 elements) is bounded to 3 CTAs per SM
     template<int L, int R, int Kind, int NW>
-    __global__ void __launch_bounds__(256, (R >= 3 ? 2 : 4)) ntt_pass_kernel(const NttPassParams p,
+    __global__ void __launch_bounds__(256, (R >= 3 ? 2 : 3)) ntt_pass_kernel(const NttPassParams p,
                                                                             const Modulus<L> m)
     {
         extern __shared__ uint32_t smem[];
