@@ -47,8 +47,10 @@ CONFIG = {
     "l2": "per-step working set 640 MiB (messages 64 MiB + ciphertexts 512 MiB + intermediates) > 129 MB L2",
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
-# kernel from an ncu capture (see profiles/); None until captured
-DOMINANT_TRAFFIC_BYTES = None
+# kernel: mean of the four launches of two fused CBD(10) transforms of 160
+# polynomials (194.3 MB), scaled by 256/160 to this batch
+# (profiles/ntt_pass_kernel_cbd_traffic_n32768_L8.md)
+DOMINANT_TRAFFIC_BYTES = 310.8e6
 
 
 def mont_mul_ops(limbs):
@@ -459,6 +461,8 @@ def main():
     butterflies = BATCH * (N // 2) * (N.bit_length() - 1)
     ops_per_launch = butterflies * mont_mul_ops(q.limbs) / per_transform
     achieved = ops_per_launch / (launch_ms * 1e-3)
+    # the batch is written once by pass A and read + written once by pass B
+    algorithmic_bytes = 3 * BATCH * N * q.limbs * 4 / per_transform
     peak = queue.int_multiply_rate()
 
     if rank == 0:
@@ -494,6 +498,14 @@ def main():
                 "traffic": DOMINANT_TRAFFIC_BYTES,
                 "peak_source": "measured live: hmpc_probe_int_multiply_rate (independent mad.lo/mad.hi chains)",
                 "ops_per_launch": ops_per_launch,
+                "tile": q.plan(N, BATCH),
+                "hbm_view": {
+                    "algorithmic_bytes_per_launch": algorithmic_bytes,
+                    "achieved_gbs": algorithmic_bytes / (launch_ms * 1e-3) / 1e9,
+                    "peak_gbs": hbm_peak_gbs()[0],
+                    "frac": algorithmic_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak_gbs()[0],
+                    "peak_source": hbm_peak_gbs()[1],
+                },
                 "launch_ms": launch_ms,
             },
             "clocks": clocks.summary(),

@@ -60,6 +60,13 @@ class Modulus:
         _lib.call("hmpc_modulus_tune", self.handle, n, batch, int(inverse), ctypes.byref(ms))
         return ms.value
 
+    def plan(self, n, batch, inverse=False):
+        """the tile shape (radix_bits, local_bits, col_bits) these transforms run with"""
+        r, lb, cb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.call("hmpc_modulus_get_plan", self.handle, n, batch, int(inverse), ctypes.byref(r), ctypes.byref(lb),
+                  ctypes.byref(cb))
+        return {"radix_bits": r.value, "local_bits": lb.value, "col_bits": cb.value}
+
     def root(self, n, inverse=False):
         out = (ctypes.c_uint32 * 16)()
         _lib.call("hmpc_modulus_root", self.handle, n, int(inverse), out)

@@ -84,9 +84,9 @@ namespace hmpc_gb300::detail
         {
             return rc;
         }
-        if (!mod || !out)
+        if (!mod)
         {
-            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus or output");
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
         }
         if (int rc = check_degree(n))
         {
@@ -95,6 +95,10 @@ namespace hmpc_gb300::detail
         if (batch == 0)
         {
             return HMPC_OK;
+        }
+        if (!out)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
         }
         Tables* t = nullptr;
         if (int rc = mod->prepare(n, &t))
@@ -292,9 +296,9 @@ namespace hmpc_gb300::detail
         {
             return rc;
         }
-        if (!mod || !out)
+        if (!mod)
         {
-            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus or output");
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null modulus");
         }
         if (int rc = check_degree(n))
         {
@@ -303,6 +307,10 @@ namespace hmpc_gb300::detail
         if (batch == 0)
         {
             return HMPC_OK;
+        }
+        if (!out)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
         }
         Tables* t = nullptr;
         if (int rc = mod->prepare(n, &t))
@@ -584,6 +592,32 @@ int hmpc_modulus_prepare(hmpc_modulus* mod, uint64_t n)
         return rc;
     }
     return mod->prepare(n, nullptr);
+}
+
+int hmpc_modulus_get_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int* radix_bits,
+                          int* local_bits, int* col_bits)
+{
+    if (!mod || !radix_bits || !local_bits || !col_bits)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    hmpc_modulus::TileChoice choice;
+    {
+        std::lock_guard<std::mutex> lock(mod->tables_mutex);
+        auto it = mod->tile_choices.find(std::make_tuple(__builtin_ctzll(n), inverse ? 1 : 0, batch));
+        if (it != mod->tile_choices.end())
+        {
+            choice = it->second;
+        }
+    }
+    *radix_bits = choice.radix_bits;
+    *local_bits = choice.local_bits;
+    *col_bits = choice.col_bits;
+    return HMPC_OK;
 }
 
 int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits,

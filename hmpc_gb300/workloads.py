@@ -87,6 +87,7 @@ def main(argv=None):
             result["tuned_ms"] = q.tune(args.n, args.batch, inverse=args.workload == "intt")
         elif args.radix_bits:
             q.set_plan(args.n, args.batch, args.workload == "intt", args.radix_bits, args.local_bits, args.col_bits)
+        result["tile"] = q.plan(args.n, args.batch, inverse=args.workload == "intt")
         x = queue.uniform(q, (args.batch,), args.n)
         out = Tensor(q, (args.batch,), args.n)
         if args.workload == "ntt":

@@ -98,6 +98,11 @@ int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root
 int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits, int local_bits,
                           int col_bits);
 int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, float* best_ms);
+/* The tile shape the transforms of (n, batch, inverse) run with: the one set
+ * or tuned for them, else the default (radix bits 3, tile bits 0, column
+ * bits 4). */
+int hmpc_modulus_get_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int* radix_bits, int* local_bits,
+                          int* col_bits);
 /* Copy a cached twiddle table (n*L words, element-major) to host memory. */
 int hmpc_modulus_twiddles(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* host_table);
 
