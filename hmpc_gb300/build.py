@@ -16,6 +16,7 @@ OUT = HERE / "_build"
 LIB = OUT / "libhmpc_gb300.so"
 INCLUDE = HERE.parent / "include"
 LIMBS = range(1, 10)
+TC_LIMBS = (2, 4, 8)  # limb counts of the tensor-core transform
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,7 +56,13 @@ def build(verbose=False, jobs=None):
         objects.append(obj)
         if _stale(obj, [CSRC / "kernels.cu", *headers]):
             steps.append(common + [f"-DHMPC_L={limbs}", "-c", str(CSRC / "kernels.cu"), "-o", str(obj)])
-    for name in ("api.cpp", "host_math.cpp", "probe.cu", "noalloc.cu", "batched.cpp", "serve.cpp", "cipher.cu"):
+    for limbs in TC_LIMBS:
+        obj = OUT / f"tensor_ntt_L{limbs}.o"
+        objects.append(obj)
+        if _stale(obj, [CSRC / "tensor_ntt.cu", *headers]):
+            steps.append(common + [f"-DHMPC_L={limbs}", "-c", str(CSRC / "tensor_ntt.cu"), "-o", str(obj)])
+    for name in ("api.cpp", "host_math.cpp", "probe.cu", "noalloc.cu", "batched.cpp", "serve.cpp", "cipher.cu",
+                 "tc.cpp"):
         obj = OUT / (name.rsplit(".", 1)[0] + ".o")
         objects.append(obj)
         if _stale(obj, [CSRC / name, *headers]):

@@ -152,6 +152,15 @@ namespace hmpc_gb300::detail
                 choice = it->second;
             }
         }
+        if (choice.radix_bits == 0)
+        {
+            // tensor-core engine; calls it does not cover run the default CUDA-core tiles
+            if (tc_applicable(mod, log_n, kind, poly_rng))
+            {
+                return run_tc_transform(ctx, mod, n, batch, inverse, kind, vx2, src, out);
+            }
+            choice = hmpc_modulus::TileChoice{};
+        }
         PlanOptions options;
         options.max_local_bits = choice.local_bits;
         options.col_bits = choice.col_bits;
@@ -431,6 +440,8 @@ int hmpc_context_destroy(hmpc_context* ctx)
         delete m;
     }
     cudaFree(ctx->workspace);
+    cudaFree(ctx->tc_workspace);
+    cudaFree(ctx->tc_error);
     delete ctx;
     return HMPC_OK;
 }
@@ -496,6 +507,16 @@ int hmpc_context_synchronize(hmpc_context* ctx)
         return rc;
     }
     HMPC_CUDA(cudaStreamSynchronize(ctx->stream), "synchronizing");
+    if (ctx->tc_error)
+    {
+        uint32_t code = 0;
+        HMPC_CUDA(cudaMemcpy(&code, ctx->tc_error, sizeof code, cudaMemcpyDeviceToHost), "reading the error word");
+        if (code)
+        {
+            HMPC_CUDA(cudaMemset(ctx->tc_error, 0, sizeof code), "clearing the error word");
+            return fail(HMPC_ERROR_TIMEOUT, "a tensor-core transform gave up waiting for its tensor core or copy");
+        }
+    }
     return HMPC_OK;
 }
 
@@ -631,8 +652,17 @@ int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inv
     {
         return rc;
     }
-    if ((radix_bits != 2 && radix_bits != 3) || local_bits < 0 || local_bits > 13 || col_bits < 0 || col_bits > 6 ||
-        (local_bits && static_cast<uint64_t>(mod->c.limbs) * 4u * smem_words(1u << local_bits) > 200 * 1024))
+    if (radix_bits == 0)
+    {
+        if (!tc_supported(mod))
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core transform needs a 2-, 4- or 8-limb modulus below "
+                                                "0.996 * 2^(32L) whose top limb is at least 32");
+        }
+    }
+    else if ((radix_bits != 2 && radix_bits != 3) || local_bits < 0 || local_bits > 13 || col_bits < 0 ||
+             col_bits > 6 ||
+             (local_bits && static_cast<uint64_t>(mod->c.limbs) * 4u * smem_words(1u << local_bits) > 200 * 1024))
     {
         return fail(HMPC_ERROR_INVALID_ARGUMENT, "tile shape out of range");
     }
@@ -682,6 +712,41 @@ int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse
     const int b0 = local_bits_for(L, def);
     float best = 1e30f;
     hmpc_modulus::TileChoice best_choice;
+    auto time_choice = [&](const hmpc_modulus::TileChoice& choice) {
+        {
+            std::lock_guard<std::mutex> lock(mod->tables_mutex);
+            mod->tile_choices[key] = choice;
+        }
+        float sample = 1e30f;
+        for (int rep = 0; rep < 4; ++rep)
+        {
+            cudaEventRecord(t0, ctx->stream);
+            if (run_transform(ctx, mod, n, batch, inverse, producer_tensor, 0, 0, buf, buf) != HMPC_OK)
+            {
+                return 1e30f;
+            }
+            cudaEventRecord(t1, ctx->stream);
+            cudaEventSynchronize(t1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, t0, t1);
+            if (rep)
+            {
+                sample = std::min(sample, ms);
+            }
+        }
+        return sample;
+    };
+    if (log_n >= 4 && tc_supported(mod))
+    {
+        hmpc_modulus::TileChoice tensor;
+        tensor.radix_bits = 0;
+        const float sample = time_choice(tensor);
+        if (sample < best)
+        {
+            best = sample;
+            best_choice = tensor;
+        }
+    }
     for (int R : {3, 2})
     {
         for (int lb = std::max(R + 2, b0 - 5); lb <= std::min(13, b0 + 1); ++lb)
@@ -692,28 +757,7 @@ int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse
             }
             for (int c : {3, 4, 5})
             {
-                {
-                    std::lock_guard<std::mutex> lock(mod->tables_mutex);
-                    mod->tile_choices[key] = {R, lb, c};
-                }
-                float sample = 1e30f;
-                for (int rep = 0; rep < 4; ++rep)
-                {
-                    cudaEventRecord(t0, ctx->stream);
-                    if (run_transform(ctx, mod, n, batch, inverse, producer_tensor, 0, 0, buf, buf) != HMPC_OK)
-                    {
-                        sample = 1e30f;
-                        break;
-                    }
-                    cudaEventRecord(t1, ctx->stream);
-                    cudaEventSynchronize(t1);
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, t0, t1);
-                    if (rep)
-                    {
-                        sample = std::min(sample, ms);
-                    }
-                }
+                const float sample = time_choice({R, lb, c});
                 if (sample < best)
                 {
                     best = sample;

@@ -10,6 +10,7 @@
 #include "chacha.cuh"
 #include "ntt.cuh"
 #include "plain.cuh"
+#include "tensor_ntt.cuh"
 
 namespace hmpc_gb300
 {
@@ -77,6 +78,39 @@ namespace hmpc_gb300
         int (*ntt_batched_blocks_per_sm)(int radix_bits, size_t smem);
         int radix_bits;
     };
+
+    // sizes of one tensor-core group kernel instantiation (TcShape)
+    struct TcShapeInfo
+    {
+        uint32_t smem = 0, a_bytes = 0, b_bytes = 0, k_pad = 0, n_mma = 0, w_in = 0, w_out = 0, d_in = 0;
+    };
+
+    // tensor-core transform kernels of one limb count (2, 4 or 8 limbs: 8, 16 or
+    // 32 digits per residue)
+    struct TcKernels
+    {
+        int digits;
+        cudaError_t (*group)(const TcGroupParams& p, int r, int in_kind, int out_kind, unsigned grid,
+                             cudaStream_t stream);
+        bool (*shape)(int r, int in_kind, int out_kind, TcShapeInfo& out);
+        cudaError_t (*gen)(const TcGenParams& p, const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*expand)(const TcExpandParams& p, const HostModulus& m, cudaStream_t stream);
+    };
+
+    const TcKernels* tc_kernels_2();
+    const TcKernels* tc_kernels_4();
+    const TcKernels* tc_kernels_8();
+
+    inline const TcKernels* tc_kernels(int limbs)
+    {
+        switch (limbs)
+        {
+        case 2: return tc_kernels_2();
+        case 4: return tc_kernels_4();
+        case 8: return tc_kernels_8();
+        default: return nullptr;
+        }
+    }
 
     const KernelTable* kernel_table_1();
     const KernelTable* kernel_table_2();

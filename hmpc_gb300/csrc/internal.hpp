@@ -28,6 +28,27 @@ namespace hmpc_gb300::detail
         uint32_t* inverse = nullptr;
         host::words root, inverse_root;
     };
+
+    // one group of the tensor-core transform: stages [s0, s0 + g), element
+    // bits below the group `lo`, `blocks` constant matrices of shape.b_bytes
+    // each at byte `offset` of the images
+    struct TcGroupPlan
+    {
+        uint32_t s0 = 0, g = 0, lo = 0;
+        uint64_t blocks = 0;
+        int in_kind = 0, out_kind = 0;
+        TcShapeInfo shape;
+        size_t offset = 0;
+    };
+
+    struct TcTables
+    {
+        std::vector<TcGroupPlan> groups;
+        uint8_t* images = nullptr;     // every group's constants (first group fed by limbs)
+        size_t bytes = 0;
+        uint8_t* first_cbd = nullptr;  // first group fed by centred binomial samples
+        TcShapeInfo cbd_shape;
+    };
 }
 
 #define HMPC_CUDA(call, what)                                                                                         \
@@ -50,6 +71,33 @@ struct hmpc_context
     uint64_t workspace_words = 0;
     uint64_t launches = 0;  // kernels launched through this context
     std::vector<hmpc_modulus*> moduli;
+    // tensor-core transforms: two digit buffers (separate from `workspace`,
+    // which callers of a transform may hold), the bounded-wait error word
+    // and the SM count that sizes the persistent grid
+    uint32_t* tc_workspace = nullptr;
+    uint64_t tc_workspace_words = 0;
+    uint32_t* tc_error = nullptr;
+    int sm_count = 0;
+
+    uint32_t* tc_scratch(uint64_t words)
+    {
+        if (words > tc_workspace_words)
+        {
+            if (tc_workspace)
+            {
+                cudaStreamSynchronize(stream);
+                cudaFree(tc_workspace);
+                tc_workspace = nullptr;
+                tc_workspace_words = 0;
+            }
+            if (cudaMalloc(&tc_workspace, words * sizeof(uint32_t)) != cudaSuccess)
+            {
+                return nullptr;
+            }
+            tc_workspace_words = words;
+        }
+        return tc_workspace;
+    }
 
     uint32_t* scratch(uint64_t words)
     {
@@ -88,6 +136,8 @@ struct hmpc_modulus
     const hmpc_gb300::KernelTable* kt = nullptr;
     uint32_t* small_table = nullptr;  // Montgomery forms of 0..64, element-major
     std::map<uint64_t, hmpc_gb300::detail::Tables> tables;
+    // tensor-core transform constants per (log2 N, inverse)
+    std::map<std::pair<int, int>, hmpc_gb300::detail::TcTables> tc_tables;
 
     ~hmpc_modulus()
     {
@@ -96,6 +146,11 @@ struct hmpc_modulus
         {
             cudaFree(kv.second.forward);
             cudaFree(kv.second.inverse);
+        }
+        for (auto& kv : tc_tables)
+        {
+            cudaFree(kv.second.images);
+            cudaFree(kv.second.first_cbd);
         }
     }
 
@@ -154,4 +209,12 @@ namespace hmpc_gb300::detail
     int run_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                   uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
     CastParams make_cast(const hmpc_modulus* dst, const hmpc_modulus* src);
+    // tensor-core engine: whether the modulus qualifies (2, 4 or 8 limbs, q
+    // below 0.996 * 2^(32L), top limb at least 32) and whether a call does
+    // (forward from a tensor or CBD(V) samples, or inverse; at least 16
+    // coefficients; no per-polynomial RNG)
+    bool tc_supported(const hmpc_modulus* mod);
+    bool tc_applicable(const hmpc_modulus* mod, int log_n, int kind, const uint32_t* poly_rng);
+    int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
+                         uint32_t vx2, const uint32_t* src, uint32_t* out);
 }

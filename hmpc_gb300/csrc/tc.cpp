@@ -1,0 +1,307 @@
+// Host side of the tensor-core transform: group plan, lazily generated
+// constant matrices per (modulus, degree, direction), and the launch sequence.
+#include <algorithm>
+#include <cmath>
+
+#include "internal.hpp"
+
+using namespace hmpc_gb300;
+using namespace hmpc_gb300::detail;
+
+namespace
+{
+    // polls of an mbarrier before a group kernel reports HMPC_ERROR_TIMEOUT;
+    // each poll is a try_wait that itself suspends for a bounded time
+    constexpr uint32_t tc_spin_limit = 1u << 20;
+
+    const TcKernels* kernels_of(const hmpc_modulus* mod)
+    {
+        return tc_kernels(mod->c.limbs);
+    }
+
+    // groups of three stages from the first stage on; the remainder (1-3
+    // stages) is the last group, whose constants are the most numerous in the
+    // forward direction (one matrix per block above it)
+    std::vector<TcGroupPlan> plan_groups(const TcKernels* k, int log_n, bool inverse)
+    {
+        const int count = (log_n + 2) / 3;
+        std::vector<TcGroupPlan> groups;
+        for (int j = 0; j < count; ++j)
+        {
+            TcGroupPlan gp;
+            gp.s0 = static_cast<uint32_t>(3 * j);
+            gp.g = static_cast<uint32_t>(j + 1 < count ? 3 : log_n - 3 * (count - 1));
+            gp.lo = inverse ? gp.s0 : static_cast<uint32_t>(log_n) - gp.s0 - gp.g;
+            gp.blocks = 1ull << (static_cast<uint32_t>(log_n) - gp.lo - gp.g);
+            gp.in_kind = j == 0 ? tc_in_limbs : tc_in_digits;
+            gp.out_kind = j + 1 == count ? tc_out_limbs : tc_out_digits;
+            k->shape(1 << gp.g, gp.in_kind, gp.out_kind, gp.shape);
+            groups.push_back(gp);
+        }
+        return groups;
+    }
+
+    // generate and expand one group's constants into `images`
+    int build_group(hmpc_context* ctx, hmpc_modulus* mod, const Tables* t, int log_n, bool inverse,
+                    const TcGroupPlan& gp, bool montgomery, uint32_t d_in, uint8_t* images, uint32_t* gx,
+                    const uint32_t* pow256)
+    {
+        const TcKernels* k = kernels_of(mod);
+        TcGenParams gen{};
+        gen.twiddles = inverse ? t->inverse : t->forward;
+        gen.gx = gx;
+        gen.blocks = gp.blocks;
+        gen.log_n = static_cast<uint32_t>(log_n);
+        gen.inverse = inverse ? 1u : 0u;
+        gen.s0 = gp.s0;
+        gen.g = gp.g;
+        gen.lo = gp.lo;
+        gen.montgomery = montgomery ? 1u : 0u;
+        HMPC_CUDA(k->gen(gen, mod->h, ctx->stream), "generating tensor-core constants");
+        TcExpandParams ex{};
+        ex.gx = gx;
+        ex.pow256 = pow256;
+        ex.images = images;
+        ex.blocks = gp.blocks;
+        ex.r = 1u << gp.g;
+        ex.dc = static_cast<uint32_t>(k->digits);
+        ex.d_in = d_in;
+        ex.n_mma = gp.shape.n_mma;
+        ex.image_bytes = gp.shape.b_bytes;
+        for (int j = 0; j < mod->c.limbs; ++j)
+        {
+            ex.half[j] = mod->c.half[static_cast<size_t>(j)];
+        }
+        HMPC_CUDA(k->expand(ex, mod->h, ctx->stream), "expanding tensor-core constants");
+        return HMPC_OK;
+    }
+
+    int prepare_tc(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, bool need_cbd, TcTables** out)
+    {
+        Tables* t = nullptr;
+        if (int rc = mod->prepare(n, &t))
+        {
+            return rc;
+        }
+        const int log_n = __builtin_ctzll(n);
+        const TcKernels* k = kernels_of(mod);
+        const int L = mod->c.limbs;
+        std::lock_guard<std::mutex> lock(mod->tables_mutex);
+        auto key = std::make_pair(log_n, inverse ? 1 : 0);
+        auto it = mod->tc_tables.find(key);
+        const bool fresh = it == mod->tc_tables.end();
+        if (!fresh && (!need_cbd || it->second.first_cbd))
+        {
+            *out = &it->second;
+            return HMPC_OK;
+        }
+        TcTables tt;
+        if (!fresh)
+        {
+            tt = it->second;
+        }
+        else
+        {
+            tt.groups = plan_groups(k, log_n, inverse);
+            size_t bytes = 0;
+            for (auto& gp : tt.groups)
+            {
+                gp.offset = bytes;
+                bytes += static_cast<size_t>(gp.blocks) * gp.shape.b_bytes;
+                bytes = (bytes + 255) & ~static_cast<size_t>(255);
+            }
+            tt.bytes = bytes;
+        }
+        // 256^a * R mod q for every digit slot
+        const uint32_t slots = static_cast<uint32_t>(k->digits + 2);
+        std::vector<uint32_t> pow256(static_cast<size_t>(slots) * L);
+        for (uint32_t a = 0; a < slots; ++a)
+        {
+            host::words v(static_cast<size_t>(a / 4 + 1), 0u);
+            v[a / 4] = 1u << (8 * (a % 4));
+            const host::words mv = host::to_mont(mod->c, v);
+            for (int j = 0; j < L; ++j)
+            {
+                pow256[static_cast<size_t>(a) * L + j] = mv[static_cast<size_t>(j)];
+            }
+        }
+        uint64_t gx_words = 0;
+        for (const auto& gp : tt.groups)
+        {
+            gx_words = std::max<uint64_t>(gx_words, (gp.blocks << (2 * gp.g)) * static_cast<uint64_t>(L));
+        }
+        uint32_t* d_pow = nullptr;
+        uint32_t* d_gx = nullptr;
+        auto cleanup = [&]() {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(d_pow);
+            cudaFree(d_gx);
+        };
+        if (cudaMalloc(&d_pow, pow256.size() * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&d_gx, gx_words * sizeof(uint32_t)) != cudaSuccess)
+        {
+            cleanup();
+            return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core generation scratch");
+        }
+        if (cudaMemcpyAsync(d_pow, pow256.data(), pow256.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                            ctx->stream) != cudaSuccess)
+        {
+            cleanup();
+            return fail(HMPC_ERROR_CUDA, "uploading digit powers");
+        }
+        if (fresh)
+        {
+            if (cudaMalloc(&tt.images, tt.bytes) != cudaSuccess)
+            {
+                cleanup();
+                return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core constants");
+            }
+            cudaMemsetAsync(tt.images, 0, tt.bytes, ctx->stream);
+            for (const auto& gp : tt.groups)
+            {
+                if (int rc = build_group(ctx, mod, t, log_n, inverse, gp, false, gp.shape.d_in, tt.images + gp.offset,
+                                         d_gx, d_pow))
+                {
+                    cleanup();
+                    cudaFree(tt.images);
+                    return rc;
+                }
+                // the generation scratch is reused by the next group
+                cudaStreamSynchronize(ctx->stream);
+            }
+        }
+        if (need_cbd && !tt.first_cbd)
+        {
+            // first forward group fed by raw samples: constants G * R
+            k->shape(8, tc_in_cbd, tc_out_digits, tt.cbd_shape);
+            TcGroupPlan gp = tt.groups.front();
+            gp.shape = tt.cbd_shape;
+            if (cudaMalloc(&tt.first_cbd, tt.cbd_shape.b_bytes) != cudaSuccess)
+            {
+                cleanup();
+                return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core constants");
+            }
+            cudaMemsetAsync(tt.first_cbd, 0, tt.cbd_shape.b_bytes, ctx->stream);
+            if (int rc = build_group(ctx, mod, t, log_n, inverse, gp, true, 1, tt.first_cbd, d_gx, d_pow))
+            {
+                cleanup();
+                return rc;
+            }
+        }
+        cleanup();
+        if (cudaGetLastError() != cudaSuccess)
+        {
+            return fail(HMPC_ERROR_CUDA, "generating tensor-core constants");
+        }
+        mod->tc_tables[key] = tt;
+        *out = &mod->tc_tables[key];
+        return HMPC_OK;
+    }
+}
+
+namespace hmpc_gb300::detail
+{
+    bool tc_supported(const hmpc_modulus* mod)
+    {
+        const int L = mod->c.limbs;
+        if (!tc_kernels(L))
+        {
+            return false;
+        }
+        // q / 2 must have 4L balanced base-256 digits: floor(q / 2) <= 0x7F7F...7F
+        host::words bound(static_cast<size_t>(L), 0x7F7F7F7Fu);
+        if (host::compare(mod->c.half, bound) > 0)
+        {
+            return false;
+        }
+        // the quotient estimate of the final reduction reads the top limb
+        return mod->c.q[static_cast<size_t>(L - 1)] >= 32u;
+    }
+
+    bool tc_applicable(const hmpc_modulus* mod, int log_n, int kind, const uint32_t* poly_rng)
+    {
+        return log_n >= 4 && !poly_rng && (kind == producer_tensor || kind == producer_cbd) && tc_supported(mod);
+    }
+
+    int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
+                         uint32_t vx2, const uint32_t* src, uint32_t* out)
+    {
+        const bool cbd = kind == producer_cbd;
+        if (cbd && (vx2 < 1 || vx2 > 64))
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "centred binomial needs 1 <= 2V <= 64");
+        }
+        TcTables* tt = nullptr;
+        if (int rc = prepare_tc(ctx, mod, n, inverse, cbd, &tt))
+        {
+            return rc;
+        }
+        const TcKernels* k = kernels_of(mod);
+        const int L = mod->c.limbs;
+        const uint64_t elements = n * batch;
+        const uint32_t w = tt->groups.front().shape.w_out;
+        const size_t stages = tt->groups.size();
+        uint32_t* digits = nullptr;
+        if (stages > 1)
+        {
+            digits = ctx->tc_scratch((stages > 2 ? 2 : 1) * static_cast<uint64_t>(w) * elements);
+            if (!digits)
+            {
+                return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core digit buffers");
+            }
+        }
+        if (!ctx->tc_error)
+        {
+            HMPC_CUDA(cudaMalloc(&ctx->tc_error, sizeof(uint32_t)), "allocating the error word");
+            HMPC_CUDA(cudaMemsetAsync(ctx->tc_error, 0, sizeof(uint32_t), ctx->stream), "clearing the error word");
+        }
+        if (!ctx->sm_count)
+        {
+            HMPC_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device),
+                      "querying the SM count");
+        }
+        // 2^(32(L-1)) / q from the top two limbs
+        const double top = static_cast<double>(mod->c.q[static_cast<size_t>(L - 1)]) +
+                           static_cast<double>(mod->c.q[static_cast<size_t>(L - 2)]) / 4294967296.0;
+        const float inv_q_top = static_cast<float>(1.0 / top);
+        const RngKey rng = ctx->rng();
+        for (size_t j = 0; j < stages; ++j)
+        {
+            const TcGroupPlan& gp = tt->groups[j];
+            TcGroupParams p{};
+            p.in = j == 0 ? src : digits + (((j - 1) & 1u) ? static_cast<uint64_t>(w) * elements : 0);
+            p.out = j + 1 == stages ? out : digits + ((j & 1u) ? static_cast<uint64_t>(w) * elements : 0);
+            p.images = (j == 0 && cbd) ? tt->first_cbd : tt->images + gp.offset;
+            p.error = ctx->tc_error;
+            p.elements = elements;
+            p.rows = batch << gp.lo;
+            p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
+            p.tiles = gp.blocks * p.tiles_per_block;
+            p.log_n = static_cast<uint32_t>(__builtin_ctzll(n));
+            p.lo = gp.lo;
+            p.spin_limit = tc_spin_limit;
+            p.rng = rng;
+            p.vx2 = vx2;
+            p.nw = (2 * vx2 + 31) / 32;
+            for (int i = 0; i < L; ++i)
+            {
+                p.q[i] = mod->c.q[static_cast<size_t>(i)];
+            }
+            p.inv_q_top = inv_q_top;
+            const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
+            const int in_kind = j == 0 ? (cbd ? static_cast<int>(tc_in_cbd) : static_cast<int>(tc_in_limbs))
+                                       : static_cast<int>(tc_in_digits);
+            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, grid, ctx->stream);
+            if (e != cudaSuccess)
+            {
+                return cuda_fail(e, "launching a tensor-core transform group");
+            }
+            ++ctx->launches;
+        }
+        if (cbd)
+        {
+            nonce_add(ctx->nonce, elements);
+        }
+        return HMPC_OK;
+    }
+}

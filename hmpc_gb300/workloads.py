@@ -74,7 +74,8 @@ def main(argv=None):
     ap.add_argument("--elements", type=int, default=1 << 24)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--tune", action="store_true", help="autotune the tile shape first")
-    ap.add_argument("--radix-bits", type=int, default=0, help="force a tile shape (with --local-bits, --col-bits)")
+    ap.add_argument("--radix-bits", type=int, default=None,
+                    help="force a tile shape (with --local-bits, --col-bits); 0 = tensor-core engine")
     ap.add_argument("--local-bits", type=int, default=0)
     ap.add_argument("--col-bits", type=int, default=4)
     args = ap.parse_args(argv)
@@ -85,7 +86,7 @@ def main(argv=None):
         q.prepare(args.n)
         if args.tune:
             result["tuned_ms"] = q.tune(args.n, args.batch, inverse=args.workload == "intt")
-        elif args.radix_bits:
+        elif args.radix_bits is not None:
             q.set_plan(args.n, args.batch, args.workload == "intt", args.radix_bits, args.local_bits, args.col_bits)
         result["tile"] = q.plan(args.n, args.batch, inverse=args.workload == "intt")
         x = queue.uniform(q, (args.batch,), args.n)

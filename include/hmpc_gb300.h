@@ -92,7 +92,10 @@ int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root
 /* Tile shape of the transforms of degree n over `batch` polynomials in one
  * direction: register radix bits (2 or 3: 4 or 8 elements per thread), tile
  * bits (log2 elements a CTA stages; 0 = by shared-memory budget) and column
- * bits (coalescing width).  No counterpart in the reference (its transform
+ * bits (coalescing width) -- or radix bits 0: the tensor-core engine (exact
+ * fp16 MMAs over 8-bit digits, 2-, 4- and 8-limb moduli below
+ * 0.996 * 2^(32L); tensor and CBD(V) producers; other calls of that shape
+ * run the default tiles).  No counterpart in the reference (its transform
  * has one schedule).  hmpc_modulus_tune times the candidates on the device
  * (scratch buffers, values irrelevant to the cost) and keeps the fastest. */
 int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits, int local_bits,

@@ -1,0 +1,140 @@
+"""Parity of the tensor-core transform engine (tile shape radix bits 0) with
+the CPU oracle: bit-exact forward and inverse transforms, fused CBD(V)
+samplers, ragged batches, in-place calls, and the fallback to the CUDA-core
+tiles for calls the engine does not cover."""
+import numpy as np
+import pytest
+
+from hmpc_gb300 import _lib
+from hmpc_gb300.comp import Queue, Tensor
+
+pytestmark = pytest.mark.gpu
+
+KEY = [0x9E3779B9, 0x7F4A7C15, 0xF39CC060, 0x5CEDC834, 0x1082276B, 0xF3A27251, 0xF86C6A11, 0x4D2A8E5B]
+Q_256 = 0xCFF479B9B12CCF05AF55BCA0D7AE005D53E20D920B577D2785F3A1F156740001  # L=8
+Q_128 = 0xE78EC7A9E37BEFBFF59DF3057EBC0001  # L=4
+Q_NTT = 0x18F25CD9A75CCBD9C146D4ABAEC00001  # examples/ntt.cpp:22, L=4, 125 bits
+P_64 = 0x8822D80623320001  # tests/expr/crypto/lhe/enc.cpp:16, L=2
+Q_192 = 0x8605423C957246B58997DEC24F688AB3DD46CB31C5700001  # L=6: not covered by the engine
+
+
+@pytest.fixture(scope="module")
+def queue():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    q = Queue(key=KEY)
+    yield q
+    q.close()
+
+
+def groups(n):
+    return (n.bit_length() - 1 + 2) // 3
+
+
+def random_residues(oracle, mod, count, seed):
+    rng = np.random.default_rng(seed)
+    words = rng.integers(0, 2**32, size=(mod.limbs, count), dtype=np.uint64).astype(np.uint32)
+    words[mod.limbs - 1] &= np.uint32((1 << (mod.bits % 32 or 32)) - 1)
+    vals = [v % mod.value for v in oracle.unplanar(words)]
+    return oracle.from_uint(mod, oracle.planar(vals, mod.limbs))
+
+
+def tensor_plan(gm, n, batch, inverse=False):
+    gm.set_plan(n, batch, inverse, radix_bits=0)
+    assert gm.plan(n, batch, inverse)["radix_bits"] == 0
+
+
+@pytest.mark.parametrize("q", [Q_256, Q_128, Q_NTT, P_64])
+@pytest.mark.parametrize("n,batch", [(16, 3), (32, 1), (64, 5), (1 << 10, 2), (1 << 12, 130), (1 << 13, 3)])
+def test_forward_and_inverse_match_oracle(queue, oracle, q, n, batch, cpu_threads):
+    om = oracle.Modulus(q)
+    gm = queue.modulus(q)
+    tensor_plan(gm, n, batch)
+    tensor_plan(gm, n, batch, inverse=True)
+    x = random_residues(oracle, om, n * batch, n + batch)
+    dx = Tensor.from_numpy(gm, x, (batch,), n)
+    before = queue.launches
+    y = queue.ntt(dx)
+    assert queue.launches - before == groups(n)
+    ref = oracle.ntt(om, n, batch, src=x, threads=cpu_threads)
+    assert np.array_equal(y.numpy(), ref)
+    z = queue.intt(y)
+    assert np.array_equal(z.numpy(), x)
+    assert _lib.call("hmpc_context_synchronize", queue.handle) == 0
+
+
+@pytest.mark.parametrize("q", [Q_256, Q_128, P_64])
+@pytest.mark.parametrize("vx2", [1, 7, 20, 64])
+def test_fused_cbd_matches_oracle(queue, oracle, q, vx2, cpu_threads):
+    om = oracle.Modulus(q)
+    gm = queue.modulus(q)
+    n, batch = 1 << 11, 5
+    tensor_plan(gm, n, batch)
+    nonce = [0xFFFFFFF0, 7, 1]
+    queue.nonce = nonce
+    y = queue.ntt_centered_binomial(gm, n, (batch,), vx2)
+    assert queue.nonce == oracle.nonce_add(nonce, n * batch)
+    ref = oracle.ntt(om, n, batch, sampler="cbd", variance_x2=vx2, key=KEY, nonce=nonce, threads=cpu_threads)
+    assert np.array_equal(y.numpy(), ref)
+
+
+def test_full_size_bgv_transform(queue, oracle, cpu_threads):
+    """the bench's transform shape: 2^15 coefficients, q 256-bit, a batch
+    spanning several 128-row tiles per constant matrix"""
+    om = oracle.Modulus(Q_256)
+    gm = queue.modulus(Q_256)
+    n, batch = 1 << 15, 260
+    tensor_plan(gm, n, batch)
+    tensor_plan(gm, n, batch, inverse=True)
+    queue.nonce = [5, 0, 0]
+    y = queue.ntt_centered_binomial(gm, n, (batch,), 20)
+    # spot-check the first and the last polynomials against the oracle
+    ref = oracle.ntt(om, n, batch, sampler="cbd", variance_x2=20, key=KEY, nonce=[5, 0, 0], threads=cpu_threads)
+    got = y.numpy()
+    assert np.array_equal(got, ref)
+    x = random_residues(oracle, om, n * 2, 77)
+    big = Tensor(gm, (batch,), n)
+    big.data.zero_()
+    big.data[:, : 2 * n] = Tensor.from_numpy(gm, x, (2,), n).data
+    z = queue.intt(queue.ntt(big))
+    assert (z.data == big.data).all().item()
+
+
+def test_in_place_and_zero(queue, oracle):
+    om = oracle.Modulus(Q_256)
+    gm = queue.modulus(Q_256)
+    n, batch = 1 << 12, 3
+    tensor_plan(gm, n, batch)
+    x = random_residues(oracle, om, n * batch, 9)
+    dx = Tensor.from_numpy(gm, x, (batch,), n)
+    queue.ntt(dx, out=dx)
+    assert np.array_equal(dx.numpy(), oracle.ntt(om, n, batch, src=x))
+    zero = Tensor.from_numpy(gm, np.zeros_like(x), (batch,), n)
+    assert not queue.ntt(zero).numpy().any()
+
+
+def test_uncovered_calls_fall_back(queue, oracle):
+    """uniform samplers, degrees below 16 and unsupported moduli run the CUDA-core tiles"""
+    gm = queue.modulus(Q_256)
+    om = oracle.Modulus(Q_256)
+    n, batch = 1 << 10, 2
+    tensor_plan(gm, n, batch)
+    queue.nonce = [1, 2, 3]
+    y = queue.ntt_uniform(gm, n, (batch,))
+    assert np.array_equal(y.numpy(), oracle.ntt(om, n, batch, sampler="uniform", key=KEY, nonce=[1, 2, 3]))
+    g192 = queue.modulus(Q_192)
+    with pytest.raises(_lib.HmpcError):
+        g192.set_plan(n, batch, False, radix_bits=0)
+    small = Tensor.from_numpy(gm, random_residues(oracle, om, 8 * 2, 3), (2,), 8)
+    gm.set_plan(8, 2, False, radix_bits=0)
+    assert np.array_equal(queue.ntt(small).numpy(), oracle.ntt(om, 8, 2, src=small.numpy()))
+
+
+def test_tuner_considers_the_engine(queue):
+    gm = queue.modulus(Q_256)
+    n, batch = 1 << 12, 64
+    ms = gm.tune(n, batch)
+    assert ms > 0
+    assert gm.plan(n, batch)["radix_bits"] in (0, 2, 3)
