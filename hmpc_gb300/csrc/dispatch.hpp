@@ -83,6 +83,7 @@ namespace hmpc_gb300
     struct TcShapeInfo
     {
         uint32_t smem = 0, a_bytes = 0, b_bytes = 0, k_pad = 0, n_mma = 0, w_in = 0, w_out = 0, d_in = 0;
+        uint32_t splits = 1;  // constant images per block (output elements split over them)
     };
 
     // tensor-core transform kernels of one limb count (2, 4 or 8 limbs: 8, 16 or
@@ -90,9 +91,9 @@ namespace hmpc_gb300
     struct TcKernels
     {
         int digits;
-        cudaError_t (*group)(const TcGroupParams& p, int r, int in_kind, int out_kind, unsigned grid,
+        cudaError_t (*group)(const TcGroupParams& p, int r, int in_kind, int out_kind, int splits, unsigned grid,
                              cudaStream_t stream);
-        bool (*shape)(int r, int in_kind, int out_kind, TcShapeInfo& out);
+        bool (*shape)(int r, int in_kind, int out_kind, int splits, TcShapeInfo& out);
         cudaError_t (*gen)(const TcGenParams& p, const HostModulus& m, cudaStream_t stream);
         cudaError_t (*expand)(const TcExpandParams& p, const HostModulus& m, cudaStream_t stream);
     };

@@ -35,7 +35,12 @@ namespace
             gp.blocks = 1ull << (static_cast<uint32_t>(log_n) - gp.lo - gp.g);
             gp.in_kind = j == 0 ? tc_in_limbs : tc_in_digits;
             gp.out_kind = j + 1 == count ? tc_out_limbs : tc_out_digits;
-            k->shape(1 << gp.g, gp.in_kind, gp.out_kind, gp.shape);
+            // a group with one block per 2^g contiguous elements (the forward
+            // transform's last, the inverse's first) has as many constant
+            // matrices as rows per matrix are few: split each over two images
+            // so that two of them fit in shared memory and stream back to back
+            const int splits = (gp.g == 3 && gp.lo == 0) ? 2 : 1;
+            k->shape(1 << gp.g, gp.in_kind, gp.out_kind, splits, gp.shape);
             groups.push_back(gp);
         }
         return groups;
@@ -66,6 +71,7 @@ namespace
         ex.r = 1u << gp.g;
         ex.dc = static_cast<uint32_t>(k->digits);
         ex.d_in = d_in;
+        ex.splits = gp.shape.splits;
         ex.n_mma = gp.shape.n_mma;
         ex.image_bytes = gp.shape.b_bytes;
         for (int j = 0; j < mod->c.limbs; ++j)
@@ -107,7 +113,7 @@ namespace
             for (auto& gp : tt.groups)
             {
                 gp.offset = bytes;
-                bytes += static_cast<size_t>(gp.blocks) * gp.shape.b_bytes;
+                bytes += static_cast<size_t>(gp.blocks) * gp.shape.splits * gp.shape.b_bytes;
                 bytes = (bytes + 255) & ~static_cast<size_t>(255);
             }
             tt.bytes = bytes;
@@ -173,7 +179,7 @@ namespace
         if (need_cbd && !tt.first_cbd)
         {
             // first forward group fed by raw samples: constants G * R
-            k->shape(8, tc_in_cbd, tc_out_digits, tt.cbd_shape);
+            k->shape(8, tc_in_cbd, tc_out_digits, 1, tt.cbd_shape);
             TcGroupPlan gp = tt.groups.front();
             gp.shape = tt.cbd_shape;
             if (cudaMalloc(&tt.first_cbd, tt.cbd_shape.b_bytes) != cudaSuccess)
@@ -276,7 +282,7 @@ namespace hmpc_gb300::detail
             p.elements = elements;
             p.rows = batch << gp.lo;
             p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
-            p.tiles = gp.blocks * p.tiles_per_block;
+            p.tiles = gp.blocks * gp.shape.splits * p.tiles_per_block;
             p.log_n = static_cast<uint32_t>(__builtin_ctzll(n));
             p.lo = gp.lo;
             p.spin_limit = tc_spin_limit;
@@ -291,7 +297,8 @@ namespace hmpc_gb300::detail
             const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
             const int in_kind = j == 0 ? (cbd ? static_cast<int>(tc_in_cbd) : static_cast<int>(tc_in_limbs))
                                        : static_cast<int>(tc_in_digits);
-            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, grid, ctx->stream);
+            const int splits = (j == 0 && cbd) ? 1 : static_cast<int>(gp.shape.splits);
+            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, grid, ctx->stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching a tensor-core transform group");

@@ -36,31 +36,31 @@ namespace hmpc_gb300
             return m;
         }
 
-        template<int R, int IN, int OUT>
+        template<int R, int IN, int OUT, int NS, bool Contig>
         cudaError_t launch(const TcGroupParams& p, unsigned grid, cudaStream_t stream)
         {
-            using S = TcShape<DC, R, IN>;
+            using S = TcShape<DC, R, IN, NS>;
             // at least half of an SM's shared memory: one CTA per SM, so a CTA's
             // two accumulators (up to all 512 TMEM columns) are always free
             constexpr uint32_t smem = S::smem > 116u * 1024u ? S::smem : 116u * 1024u;
             static std::once_flag once;
             static cudaError_t configured = cudaSuccess;
             std::call_once(once, [] {
-                configured = cudaFuncSetAttribute(tc_group_kernel<DC, R, IN, OUT>,
+                configured = cudaFuncSetAttribute(tc_group_kernel<DC, R, IN, OUT, NS, Contig>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             });
             if (configured != cudaSuccess)
             {
                 return configured;
             }
-            tc_group_kernel<DC, R, IN, OUT><<<grid, tc_threads, smem, stream>>>(p);
+            tc_group_kernel<DC, R, IN, OUT, NS, Contig><<<grid, tc_threads + 32, smem, stream>>>(p);
             return cudaGetLastError();
         }
 
-        template<int R, int IN>
+        template<int R, int IN, int NS>
         void fill(TcShapeInfo& out)
         {
-            using S = TcShape<DC, R, IN>;
+            using S = TcShape<DC, R, IN, NS>;
             out.smem = S::smem;
             out.a_bytes = S::a_bytes;
             out.b_bytes = S::b_bytes;
@@ -69,57 +69,72 @@ namespace hmpc_gb300
             out.w_in = S::w_in;
             out.w_out = S::w_out;
             out.d_in = S::d_in;
+            out.splits = NS;
         }
 
-        cudaError_t group(const TcGroupParams& p, int r, int in_kind, int out_kind, unsigned grid,
-                          cudaStream_t stream)
+        // the instantiated shapes: every (R, input, output, splits, contiguous) a plan uses
+        template<typename F>
+        bool dispatch(int r, int in_kind, int out_kind, int splits, bool contig, F& f)
         {
             if (out_kind == tc_out_digits && r == 8)
             {
-                switch (in_kind)
-                {
-                case tc_in_limbs: return launch<8, tc_in_limbs, tc_out_digits>(p, grid, stream);
-                case tc_in_cbd: return launch<8, tc_in_cbd, tc_out_digits>(p, grid, stream);
-                case tc_in_digits: return launch<8, tc_in_digits, tc_out_digits>(p, grid, stream);
-                default: break;
-                }
+                if (in_kind == tc_in_limbs && splits == 1 && !contig) return f.template run<8, tc_in_limbs, tc_out_digits, 1, false>();
+                if (in_kind == tc_in_limbs && splits == 2 && contig) return f.template run<8, tc_in_limbs, tc_out_digits, 2, true>();
+                if (in_kind == tc_in_cbd && splits == 1 && !contig) return f.template run<8, tc_in_cbd, tc_out_digits, 1, false>();
+                if (in_kind == tc_in_digits && splits == 1 && !contig) return f.template run<8, tc_in_digits, tc_out_digits, 1, false>();
             }
             if (out_kind == tc_out_limbs && in_kind == tc_in_digits)
             {
-                switch (r)
-                {
-                case 2: return launch<2, tc_in_digits, tc_out_limbs>(p, grid, stream);
-                case 4: return launch<4, tc_in_digits, tc_out_limbs>(p, grid, stream);
-                case 8: return launch<8, tc_in_digits, tc_out_limbs>(p, grid, stream);
-                default: break;
-                }
-            }
-            return cudaErrorInvalidValue;
-        }
-
-        bool shape(int r, int in_kind, int out_kind, TcShapeInfo& out)
-        {
-            if (out_kind == tc_out_digits && r == 8)
-            {
-                switch (in_kind)
-                {
-                case tc_in_limbs: fill<8, tc_in_limbs>(out); return true;
-                case tc_in_cbd: fill<8, tc_in_cbd>(out); return true;
-                case tc_in_digits: fill<8, tc_in_digits>(out); return true;
-                default: return false;
-                }
-            }
-            if (out_kind == tc_out_limbs && in_kind == tc_in_digits)
-            {
-                switch (r)
-                {
-                case 2: fill<2, tc_in_digits>(out); return true;
-                case 4: fill<4, tc_in_digits>(out); return true;
-                case 8: fill<8, tc_in_digits>(out); return true;
-                default: return false;
-                }
+                if (r == 8 && splits == 1 && !contig) return f.template run<8, tc_in_digits, tc_out_limbs, 1, false>();
+                if (r == 8 && splits == 2 && contig) return f.template run<8, tc_in_digits, tc_out_limbs, 2, true>();
+                if (r == 4 && splits == 1) return contig ? f.template run<4, tc_in_digits, tc_out_limbs, 1, true>()
+                                                         : f.template run<4, tc_in_digits, tc_out_limbs, 1, false>();
+                if (r == 2 && splits == 1) return contig ? f.template run<2, tc_in_digits, tc_out_limbs, 1, true>()
+                                                         : f.template run<2, tc_in_digits, tc_out_limbs, 1, false>();
             }
             return false;
+        }
+
+        struct Launcher
+        {
+            const TcGroupParams& p;
+            unsigned grid;
+            cudaStream_t stream;
+            cudaError_t e;
+
+            template<int R, int IN, int OUT, int NS, bool Contig>
+            bool run()
+            {
+                e = launch<R, IN, OUT, NS, Contig>(p, grid, stream);
+                return true;
+            }
+        };
+
+        struct Filler
+        {
+            TcShapeInfo& out;
+
+            template<int R, int IN, int OUT, int NS, bool Contig>
+            bool run()
+            {
+                fill<R, IN, NS>(out);
+                return true;
+            }
+        };
+
+        cudaError_t group(const TcGroupParams& p, int r, int in_kind, int out_kind, int splits, unsigned grid,
+                          cudaStream_t stream)
+        {
+            Launcher f{p, grid, stream, cudaErrorInvalidValue};
+            dispatch(r, in_kind, out_kind, splits, p.lo == 0, f);
+            return f.e;
+        }
+
+        bool shape(int r, int in_kind, int out_kind, int splits, TcShapeInfo& out)
+        {
+            Filler f{out};
+            return dispatch(r, in_kind, out_kind, splits, splits == 2, f) ||
+                   dispatch(r, in_kind, out_kind, splits, false, f) || dispatch(r, in_kind, out_kind, splits, true, f);
         }
 
         unsigned blocks_for(uint64_t threads)

@@ -71,11 +71,11 @@ namespace hmpc_gb300
     {
         const uint32_t* in;        // digit or limb planes, `elements` words each
         uint32_t* out;             // digit or limb planes
-        const uint8_t* images;     // per block: the constant operand in its shared-memory layout
+        const uint8_t* images;     // per (block, N-split): the constant operand in its shared-memory layout
         uint32_t* error;           // set when a bounded wait runs out
         uint64_t elements;         // batch * N
         uint64_t rows;             // rows per block: batch << lo
-        uint64_t tiles;            // blocks * tiles_per_block
+        uint64_t tiles;            // blocks * NS * tiles_per_block
         uint32_t tiles_per_block;
         uint32_t log_n;
         uint32_t lo;               // column bits below the group's element bits
@@ -87,7 +87,11 @@ namespace hmpc_gb300
         float inv_q_top;           // 2^(32(L-1)) / q
     };
 
-    template<int DC, int R, int IN>
+    // Sizes of one group kernel.  NS splits a block's R output elements over
+    // NS constant images (N = R / NS * DC columns each); NBUF constant buffers
+    // (two when they fit) let the next block's constants arrive while the
+    // current block computes.
+    template<int DC, int R, int IN, int NS>
     struct TcShape
     {
         static constexpr int g = R == 8 ? 3 : (R == 4 ? 2 : 1);
@@ -97,11 +101,14 @@ namespace hmpc_gb300
         static constexpr int d_eff = IN == tc_in_cbd ? 1 : (R == 8 ? d_in : (R == 4 ? (d_in + 1) / 2 * 2 : w_in * 4));
         static constexpr int k_real = R * d_eff;
         static constexpr int k_pad = (k_real + 15) / 16 * 16;
-        static constexpr int n_mma = (R * DC + 15) / 16 * 16;
+        static constexpr int outputs = R / NS;  // output elements per N-split
+        static constexpr int n_mma = (outputs * DC + 15) / 16 * 16;
         static constexpr int cols = n_mma <= 32 ? 32 : (n_mma <= 64 ? 64 : (n_mma <= 128 ? 128 : 256));
         static constexpr uint32_t a_bytes = tc_rows * k_pad * 2;
         static constexpr uint32_t b_bytes = n_mma * k_pad * 2;
-        static constexpr uint32_t smem = a_bytes + b_bytes + 64;
+        static constexpr uint32_t control_bytes = 128;  // 8 mbarriers, the TMEM address, the abort flag
+        static constexpr int nbuf = a_bytes + 2 * b_bytes + control_bytes <= 227u * 1024u ? 2 : 1;
+        static constexpr uint32_t smem = a_bytes + nbuf * b_bytes + control_bytes;
         static constexpr int w_out = (DC + 2 + 3) / 4;
         static constexpr uint32_t lbo_a = tc_rows / 8 * 128;
         static constexpr uint32_t lbo_b = n_mma / 8 * 128;
@@ -131,49 +138,90 @@ namespace hmpc_gb300
         asm volatile("st.shared.u32 [%0], %1;" ::"r"(tc::smem_u32(p)), "r"(a) : "memory");
     }
 
+    // position of a tile in the CTA's contiguous range, advanced without division
+    struct TcCursor
+    {
+        uint64_t hb;   // block * NS + split
+        uint32_t mt;   // 128-row tile within the block
+        uint32_t jb;   // index of the block in this CTA's range
+
+        __device__ __forceinline__ TcCursor next(uint32_t tiles_per_block) const
+        {
+            TcCursor c = *this;
+            if (++c.mt == tiles_per_block)
+            {
+                c.mt = 0;
+                ++c.hb;
+                ++c.jb;
+            }
+            return c;
+        }
+    };
+
     struct TcRow
     {
         bool ok;
         uint64_t base;  // element index of m = 0
         uint64_t poly;
-        uint64_t col;
     };
 
     template<int G>
-    __device__ __forceinline__ TcRow tc_row(const TcGroupParams& p, uint64_t tile, uint32_t row)
+    __device__ __forceinline__ TcRow tc_row(const TcGroupParams& p, uint64_t h, uint32_t mt, uint32_t row)
     {
-        const uint64_t h = tile / p.tiles_per_block;
-        const uint64_t rho = (tile - h * p.tiles_per_block) * tc_rows + row;
+        const uint64_t rho = static_cast<uint64_t>(mt) * tc_rows + row;
         TcRow r;
         r.ok = rho < p.rows;
         r.poly = rho >> p.lo;
-        r.col = rho & ((1ull << p.lo) - 1ull);
-        r.base = (r.poly << p.log_n) + (h << (p.lo + G)) + r.col;
+        r.base = (r.poly << p.log_n) + (h << (p.lo + G)) + (rho & ((1ull << p.lo) - 1ull));
         return r;
     }
 
     // loader of digit / limb tiles: thread (row, half) owns words [half * WH, ...) of the row's R elements
-    template<int DC, int R, int IN>
+    template<int DC, int R, int IN, int NS>
     struct TcLoader
     {
-        using S = TcShape<DC, R, IN>;
+        using S = TcShape<DC, R, IN, NS>;
         static constexpr int wh = S::w_in > 0 ? (S::w_in + 1) / 2 : 1;
         uint32_t v[wh][R];
 
-        __device__ __forceinline__ void load(const TcGroupParams& p, uint64_t tile, uint32_t row, uint32_t half)
+        __device__ __forceinline__ void load(const TcGroupParams& p, uint64_t h, uint32_t mt, uint32_t row,
+                                             uint32_t half)
         {
-            const TcRow r = tc_row<S::g>(p, tile, row);
+            const TcRow r = tc_row<S::g>(p, h, mt, row);
+            const uint32_t* rp = p.in + r.base;
+            const bool contiguous = p.lo == 0;  // the row's R elements are adjacent: vector loads
 #pragma unroll
             for (int wi = 0; wi < wh; ++wi)
             {
                 const uint32_t w = half * wh + wi;
-#pragma unroll
-                for (int m = 0; m < R; ++m)
+                const bool live = r.ok && w < static_cast<uint32_t>(S::w_in);
+                const uint32_t* wp = rp + w * p.elements;
+                if (live && contiguous)
                 {
-                    v[wi][m] = 0u;
-                    if (r.ok && w < static_cast<uint32_t>(S::w_in))
+                    if constexpr (R == 8)
                     {
-                        v[wi][m] = __ldg(p.in + w * p.elements + r.base + (static_cast<uint64_t>(m) << p.lo));
+                        const uint4 a = __ldg(reinterpret_cast<const uint4*>(wp));
+                        const uint4 b = __ldg(reinterpret_cast<const uint4*>(wp) + 1);
+                        v[wi][0] = a.x; v[wi][1] = a.y; v[wi][2] = a.z; v[wi][3] = a.w;
+                        v[wi][4] = b.x; v[wi][5] = b.y; v[wi][6] = b.z; v[wi][7] = b.w;
+                    }
+                    else if constexpr (R == 4)
+                    {
+                        const uint4 a = __ldg(reinterpret_cast<const uint4*>(wp));
+                        v[wi][0] = a.x; v[wi][1] = a.y; v[wi][2] = a.z; v[wi][3] = a.w;
+                    }
+                    else
+                    {
+                        const uint2 a = __ldg(reinterpret_cast<const uint2*>(wp));
+                        v[wi][0] = a.x; v[wi][1] = a.y;
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int m = 0; m < R; ++m)
+                    {
+                        v[wi][m] = live ? __ldg(wp + (static_cast<uint64_t>(m) << p.lo)) : 0u;
                     }
                 }
             }
@@ -238,42 +286,34 @@ namespace hmpc_gb300
     // (m, m + 4) of a row come from one generator with counter = poly * N +
     // index of the first element, first draw for m, second for m + 4
     // (number_theoretic_transform.hpp:316-329, comp/queue.hpp:191-212)
-    __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, uint8_t* sa, uint64_t tile, uint32_t row,
+    __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t row,
                                                  uint32_t half)
     {
-        const TcRow r = tc_row<3>(p, tile, row);
+        const TcRow r = tc_row<3>(p, 0, mt, row);
         int e_u[2] = {0, 0}, e_v[2] = {0, 0};
         if (r.ok)
         {
             const int count = 2 * static_cast<int>(p.vx2);
+            const int nw = static_cast<int>(p.nw);
 #pragma unroll
             for (int j = 0; j < 2; ++j)
             {
-                const uint64_t idx_u = r.base - (r.poly << p.log_n) + (static_cast<uint64_t>(2 * half + j) << p.lo);
+                const uint64_t idx = r.base + (static_cast<uint64_t>(2 * half + j) << p.lo);
                 uint32_t w[8];
-                chacha_stream<8>(p.rng, static_cast<uint32_t>((r.poly << p.log_n) + idx_u), w);
+                chacha_stream<8>(p.rng, static_cast<uint32_t>(idx), w);
                 int a = 0, b = 0;
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
                 {
-                    const int iu = i;               // word i of the first sample
-                    const int iv = i - static_cast<int>(p.nw);  // word of the second sample
+                    const int iv = i - nw;  // word of the second sample
                     uint32_t mu = 0u, mv = 0u;
-                    if (iu < static_cast<int>(p.nw))
+                    if (i < nw)
                     {
-                        mu = 0xffffffffu;
-                        if (iu == static_cast<int>(p.nw) - 1 && (count & 31))
-                        {
-                            mu = (1u << (count & 31)) - 1u;
-                        }
+                        mu = (i == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
                     }
-                    else if (iv < static_cast<int>(p.nw))
+                    else if (iv < nw)
                     {
-                        mv = 0xffffffffu;
-                        if (iv == static_cast<int>(p.nw) - 1 && (count & 31))
-                        {
-                            mv = (1u << (count & 31)) - 1u;
-                        }
+                        mv = (iv == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
                     }
                     a += __popc(w[i] & mu);
                     b += __popc(w[i] & mv);
@@ -294,20 +334,27 @@ namespace hmpc_gb300
         return __byte_perm(__byte_perm(b0, b1, 0x0040), __byte_perm(b2, b3, 0x0040), 0x5410);
     }
 
-    // carry of exact f32 column sums into balanced base-256 digits, all in f32:
-    // t = s + carry + 128; c = floor(t / 256); digit + 128 = t - 256 c
+    // Carry of exact f32 column sums into balanced base-256 digits, in f32.
+    // With t = s + carry + 128 the digit is t mod 256 - 128 and the next carry
+    // floor(t / 256).  The state x = floor(t / 256) + 2^23 also equals
+    // (next carry + 128) + C with C = 2^23 + 2^15, so the next t + C is s + x:
+    // four exact operations per digit (every value an integer below 2^24).
     struct DigitCarry
     {
-        float cp = 128.0f;  // carry + 128
+        float x = 8421504.0f;  // carry 0: 128 + C
 
         __device__ __forceinline__ uint32_t step(float s)
         {
-            const float t = s + cp;
-            const float x = __fmaf_rd(t, 0.00390625f, 12582912.0f);
-            const float c = x - 12582912.0f;
-            const float d = __fmaf_rn(-256.0f, c, t);
-            cp = c + 128.0f;
-            return __float_as_uint(d + 8388608.0f);  // low byte = digit + 128
+            const float tc = s + x;                        // t + C
+            x = __fmaf_rd(tc, 0.00390625f, 8388608.0f);    // floor((t + C) / 256) + 2^23
+            const float z = x - 8421376.0f;                // next carry + 128
+            return __float_as_uint(__fmaf_rn(-256.0f, z, tc));  // 2^23 + digit + 128
+        }
+
+        // the carry out of the last digit
+        __device__ __forceinline__ int carry() const
+        {
+            return static_cast<int>(__float_as_uint(x) - 0x4B000000u) - 32896;
         }
     };
 
@@ -318,7 +365,7 @@ namespace hmpc_gb300
         tc::tmem_load<DC>(taddr, s);
     }
 
-    // the signed value sum_j x_j 2^(32 j) + top 2^(32 L), |value / q| < 2^17,
+    // the signed value sum_j x_j 2^(32 j) + top 2^(32 L), |value / q| < 2^15,
     // reduced into [0, q)
     template<int L>
     __device__ __forceinline__ void tc_reduce(uint32_t (&x)[L], int top, const TcGroupParams& p)
@@ -373,24 +420,50 @@ namespace hmpc_gb300
         }
     }
 
-    template<int DC, int R, int OUT>
-    __device__ __forceinline__ void tc_epilogue(const TcGroupParams& p, uint32_t tmem, uint64_t tile, uint32_t warp,
-                                                uint32_t lane)
+    template<int Per>
+    __device__ __forceinline__ void store_run(uint32_t* p, const uint32_t (&v)[Per])
+    {
+        if constexpr (Per == 4)
+        {
+            *reinterpret_cast<uint4*>(p) = make_uint4(v[0], v[1], v[2], v[3]);
+        }
+        else if constexpr (Per == 2)
+        {
+            *reinterpret_cast<uint2*>(p) = make_uint2(v[0], v[1]);
+        }
+        else
+        {
+            p[0] = v[0];
+        }
+    }
+
+    // carry the accumulator of one tile out of TMEM: each thread owns one row
+    // and Per consecutive output elements of the block's split; Contig: the
+    // row's elements are adjacent (no column bits), stored as vectors
+    template<int DC, int R, int OUT, int NS, bool Contig>
+    __device__ __forceinline__ void tc_epilogue(const TcGroupParams& p, uint32_t tmem, const TcCursor& cur,
+                                                uint32_t warp, uint32_t lane)
     {
         constexpr int g = R == 8 ? 3 : (R == 4 ? 2 : 1);
         constexpr int L = DC / 4;
         constexpr int W = (DC + 2 + 3) / 4;
+        constexpr int outputs = R / NS;
+        constexpr int per = outputs / 2;
+        constexpr int words_out = OUT == tc_out_digits ? W : L;
         const uint32_t lg = warp & 3u;
         const uint32_t row = 32u * lg + lane;
-        const TcRow r = tc_row<g>(p, tile, row);
-        constexpr int per = R / 2;
-        const uint32_t k0 = (warp >> 2) * per;
-#pragma unroll 1
+        const uint64_t h = cur.hb / NS;
+        const uint32_t split = static_cast<uint32_t>(cur.hb % NS);
+        const TcRow r = tc_row<g>(p, h, cur.mt, row);
+        const uint32_t kl0 = (warp >> 2) * per;      // first local output of this thread
+        const uint32_t k0 = split * outputs + kl0;   // its element index in the group
+        uint32_t* op = p.out + r.base;
+        uint32_t res[Contig ? words_out : 1][Contig ? per : 1];
+#pragma unroll
         for (int kk = 0; kk < per; ++kk)
         {
-            const uint32_t k = k0 + kk;
             uint32_t s[DC];
-            tc_load_sums<DC>(tmem + ((32u * lg) << 16) + k * DC, s);
+            tc_load_sums<DC>(tmem + ((32u * lg) << 16) + (kl0 + kk) * DC, s);
             tc::tmem_load_wait();
             DigitCarry carry;
             uint32_t words[W];
@@ -404,20 +477,11 @@ namespace hmpc_gb300
                     words[b >> 2] = pack_bytes(bb[0], bb[1], bb[2], bb[3]);
                 }
             }
-            const uint64_t e = r.base + (static_cast<uint64_t>(k) << p.lo);
             if constexpr (OUT == tc_out_digits)
             {
                 const uint32_t c0 = carry.step(0.0f);
                 const uint32_t c1 = carry.step(0.0f);
                 words[DC / 4] = pack_bytes(c0, c1, 0x80u, 0x80u);
-                if (r.ok)
-                {
-#pragma unroll
-                    for (int w = 0; w < W; ++w)
-                    {
-                        p.out[w * p.elements + e] = words[w];
-                    }
-                }
             }
             else
             {
@@ -431,48 +495,106 @@ namespace hmpc_gb300
                     x[j] = static_cast<uint32_t>(d);
                     borrow = static_cast<uint32_t>(d >> 63);
                 }
-                const int top = __float2int_rn(carry.cp - 128.0f) - static_cast<int>(borrow);
-                tc_reduce<L>(x, top, p);
-                if (r.ok)
-                {
+                tc_reduce<L>(x, carry.carry() - static_cast<int>(borrow), p);
 #pragma unroll
-                    for (int j = 0; j < L; ++j)
-                    {
-                        p.out[j * p.elements + e] = x[j];
-                    }
+                for (int j = 0; j < L; ++j)
+                {
+                    words[j] = x[j];
+                }
+            }
+            if constexpr (Contig)
+            {
+#pragma unroll
+                for (int w = 0; w < words_out; ++w)
+                {
+                    res[w][kk] = words[w];
+                }
+            }
+            else if (r.ok)
+            {
+                const uint64_t e = static_cast<uint64_t>(k0 + kk) << p.lo;
+#pragma unroll
+                for (int w = 0; w < words_out; ++w)
+                {
+                    op[w * p.elements + e] = words[w];
+                }
+            }
+        }
+        if constexpr (Contig)
+        {
+            if (r.ok)
+            {
+#pragma unroll
+                for (int w = 0; w < words_out; ++w)
+                {
+                    store_run<per>(op + w * p.elements + k0, res[w]);
                 }
             }
         }
     }
 
-    template<int DC, int R, int IN, int OUT>
-    __global__ void __launch_bounds__(tc_threads, 1) tc_group_kernel(const TcGroupParams p)
+    __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
     {
-        using S = TcShape<DC, R, IN>;
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+    }
+
+    // One CTA per SM, persistent over a contiguous range of tiles, warp-specialised:
+    // warps 0-7 convert each 128-row digit tile into shared memory and carry
+    // accumulators out of TMEM; one thread of warp 8 streams the constant
+    // operands (bulk copies) and issues the MMAs.  mbarriers hand over the
+    // digit tile (full: 256 arrivals; empty: MMA commit), the two TMEM
+    // accumulators (full: MMA commit; empty: 256 arrivals) and the constant
+    // buffers (transaction count).  Every wait is bounded; a timeout sets the
+    // error word and both sides leave their loops.
+    template<int DC, int R, int IN, int OUT, int NS, bool Contig>
+    __global__ void __launch_bounds__(tc_threads + 32, 1) tc_group_kernel(const TcGroupParams p)
+    {
+        using S = TcShape<DC, R, IN, NS>;
+        constexpr int NBUF = S::nbuf;
         extern __shared__ __align__(1024) uint8_t tc_smem[];
-        uint8_t* sb = tc_smem;
-        uint8_t* sa = tc_smem + S::b_bytes;
-        uint64_t* bars = reinterpret_cast<uint64_t*>(sa + S::a_bytes);  // [0] operand B, [1..2] accumulators
-        uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
+        uint8_t* sb = tc_smem;                           // NBUF constant buffers
+        uint8_t* sa = tc_smem + NBUF * S::b_bytes;       // the digit tile
+        uint64_t* bars = reinterpret_cast<uint64_t*>(sa + S::a_bytes);
+        uint64_t* bar_b = bars;           // [2] constants full
+        uint64_t* bar_a_full = bars + 2;  // digit tile stored (256 arrivals)
+        uint64_t* bar_a_empty = bars + 3; // MMAs of the tile complete (commit)
+        uint64_t* bar_acc_full = bars + 4;   // [2] accumulator ready (commit)
+        uint64_t* bar_acc_empty = bars + 6;  // [2] accumulator read out (256 arrivals)
+        uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
         volatile uint32_t* abort_flag = tslot + 1;
+        static_assert(8 * sizeof(uint64_t) + 2 * sizeof(uint32_t) <= S::control_bytes, "control block");
 
         const uint32_t tid = threadIdx.x;
         const uint32_t warp = tid >> 5, lane = tid & 31u;
-        const uint32_t row = tid & (tc_rows - 1), half = tid >> 7;
 
         const uint64_t t_begin = p.tiles * blockIdx.x / gridDim.x;
         const uint64_t t_end = p.tiles * (blockIdx.x + 1) / gridDim.x;
+        const uint64_t count = t_end - t_begin;
+        const uint32_t tpb = p.tiles_per_block;
+        const uint64_t hb_first = t_begin / tpb;
+        const uint64_t hb_last = count ? (t_end - 1) / tpb : hb_first;
+        const TcCursor first{hb_first, static_cast<uint32_t>(t_begin - hb_first * tpb), 0};
 
         // K padding of the A tile stays zero
-        for (uint32_t u = tid; u < (S::k_pad - S::k_real) / 8 * tc_rows; u += tc_threads)
+        constexpr uint32_t pad_units = static_cast<uint32_t>(S::k_pad - S::k_real) / 8 * tc_rows;
+        if constexpr (pad_units > 0)
         {
-            st_shared_v4(sa + tc::operand_offset(u % tc_rows, S::k_real + 8 * (u / tc_rows), tc_rows), 0, 0, 0, 0);
+            for (uint32_t u = tid; u < pad_units; u += tc_threads + 32)
+            {
+                st_shared_v4(sa + tc::operand_offset(u % tc_rows, S::k_real + 8 * (u / tc_rows), tc_rows), 0, 0, 0,
+                             0);
+            }
         }
         if (tid == 0)
         {
-            tc::mbar_init(&bars[0], 1);
-            tc::mbar_init(&bars[1], 1);
-            tc::mbar_init(&bars[2], 1);
+            tc::mbar_init(&bar_b[0], 1);
+            tc::mbar_init(&bar_b[1], 1);
+            tc::mbar_init(bar_a_full, tc_threads);
+            tc::mbar_init(bar_a_empty, 1);
+            tc::mbar_init(&bar_acc_full[0], 1);
+            tc::mbar_init(&bar_acc_full[1], 1);
+            tc::mbar_init(&bar_acc_empty[0], tc_threads);
+            tc::mbar_init(&bar_acc_empty[1], tc_threads);
             *abort_flag = 0;
             tc::mbar_init_fence();
         }
@@ -480,136 +602,172 @@ namespace hmpc_gb300
         {
             tc::tmem_alloc(tslot, 2 * S::cols);
         }
+        tc::fence_proxy_async();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
         const uint32_t tmem = *tslot;
-        constexpr uint32_t idesc = tc::f16_instr_descriptor(tc_rows, S::n_mma);
 
-        uint32_t phase_b = 0, phase_acc = 0;  // bit i: parity of accumulator i
-        uint64_t cur_block = ~0ull;
-        bool failed = false;
-
-        auto issue_b = [&](uint64_t block) {
-            tc::mbar_arrive_expect_tx(&bars[0], S::b_bytes);
-            tc::bulk_g2s(sb, p.images + block * S::b_bytes, S::b_bytes, &bars[0]);
-        };
-        auto issue_mma = [&](uint32_t buf, bool wait_b) {
-            // thread 0 only
-            if (wait_b)
-            {
-                if (!tc::mbar_wait(&bars[0], phase_b, p.spin_limit))
-                {
-                    atomicExch(p.error, 1u);
-                    *abort_flag = 1;
-                }
-                phase_b ^= 1u;
-            }
-            tc::fence_after_sync();
-            const uint32_t a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
-#pragma unroll
-            for (int ks = 0; ks < S::k_pad / 16; ++ks)
-            {
-                tc::mma_f16(tmem + buf * S::cols, tc::smem_descriptor(a0 + ks * 2 * S::lbo_a, S::lbo_a, 128),
-                            tc::smem_descriptor(b0 + ks * 2 * S::lbo_b, S::lbo_b, 128), idesc, ks > 0);
-            }
-            tc::mma_commit(&bars[1 + buf]);
+        auto give_up = [&](uint32_t code) {
+            atomicExch(p.error, code);
+            *abort_flag = 1;
         };
 
-        TcLoader<DC, R, IN> loader;
-        if (t_begin < t_end)
+        if (warp == tc_threads / 32)
         {
-            // prologue: tile t_begin into accumulator 0
-            cur_block = t_begin / p.tiles_per_block;
-            if (tid == 0)
+            // ------------------------------------------------ MMA and copies
+            if (lane == 0 && count)
             {
-                issue_b(cur_block);
-            }
-            if constexpr (IN == tc_in_cbd)
-            {
-                tc_store_cbd(p, sa, t_begin, row, half);
-            }
-            else
-            {
-                loader.load(p, t_begin, row, half);
-                loader.store(sa, row, half);
-            }
-            tc::fence_proxy_async();
-            __syncthreads();
-            if constexpr (IN != tc_in_cbd)
-            {
-                if (t_begin + 1 < t_end)
+                constexpr uint32_t idesc = tc::f16_instr_descriptor(tc_rows, S::n_mma);
+                auto issue_b = [&](uint32_t jb) {
+                    const uint32_t buf = jb % NBUF;
+                    tc::mbar_arrive_expect_tx(&bar_b[buf], S::b_bytes);
+                    tc::bulk_g2s(sb + buf * S::b_bytes, p.images + (hb_first + jb) * S::b_bytes, S::b_bytes,
+                                 &bar_b[buf]);
+                };
+                for (uint32_t j = 0; j < static_cast<uint32_t>(NBUF); ++j)
                 {
-                    loader.load(p, t_begin + 1, row, half);
-                }
-            }
-            if (tid == 0)
-            {
-                issue_mma(0, true);
-            }
-        }
-        for (uint64_t t = t_begin; t < t_end; ++t)
-        {
-            const uint32_t buf = static_cast<uint32_t>((t - t_begin) & 1u);
-            // accumulator of tile t complete (warp-uniform bounded wait)
-            uint32_t ok = 1;
-            if (lane == 0)
-            {
-                ok = tc::mbar_wait(&bars[1 + buf], (phase_acc >> buf) & 1u, p.spin_limit) ? 1u : 0u;
-            }
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            phase_acc ^= 1u << buf;
-            if (!ok)
-            {
-                atomicExch(p.error, 2u);
-                *abort_flag = 1;
-            }
-            tc::fence_after_sync();
-            if (t + 1 < t_end)
-            {
-                const uint64_t next_block = (t + 1) / p.tiles_per_block;
-                const bool new_b = next_block != cur_block;
-                if (new_b && tid == 0)
-                {
-                    issue_b(next_block);  // the MMAs reading the old operand are complete
-                }
-                cur_block = next_block;
-                if constexpr (IN == tc_in_cbd)
-                {
-                    tc_store_cbd(p, sa, t + 1, row, half);
-                }
-                else
-                {
-                    loader.store(sa, row, half);
-                }
-                tc::fence_proxy_async();
-                tc::fence_before_sync();
-                __syncthreads();
-                if (*abort_flag)
-                {
-                    failed = true;
-                    break;
-                }
-                if constexpr (IN != tc_in_cbd)
-                {
-                    if (t + 2 < t_end)
+                    if (hb_first + j <= hb_last)
                     {
-                        loader.load(p, t + 2, row, half);
+                        issue_b(j);
                     }
                 }
-                if (tid == 0)
+                TcCursor cur = first;
+                uint32_t prev_jb = ~0u;
+                for (uint64_t i = 0; i < count && !*abort_flag; ++i)
                 {
-                    issue_mma(buf ^ 1u, new_b);
+                    const uint32_t acc = static_cast<uint32_t>(i & 1u);
+                    if (cur.jb != prev_jb)
+                    {
+                        if (i > 0 && hb_first + prev_jb + NBUF <= hb_last)
+                        {
+                            // the previous block's buffer is free once its last MMAs completed
+                            if (!tc::mbar_wait(bar_a_empty, static_cast<uint32_t>((i - 1) & 1u), p.spin_limit))
+                            {
+                                give_up(3);
+                                break;
+                            }
+                            issue_b(prev_jb + NBUF);
+                        }
+                        const uint32_t buf = cur.jb % NBUF;
+                        if (!tc::mbar_wait(&bar_b[buf], (cur.jb / NBUF) & 1u, p.spin_limit))
+                        {
+                            give_up(1);
+                            break;
+                        }
+                        prev_jb = cur.jb;
+                    }
+                    if (!tc::mbar_wait(bar_a_full, static_cast<uint32_t>(i & 1u), p.spin_limit))
+                    {
+                        give_up(4);
+                        break;
+                    }
+                    if (i >= 2 && !tc::mbar_wait(&bar_acc_empty[acc], static_cast<uint32_t>(((i - 2) >> 1) & 1u),
+                                                 p.spin_limit))
+                    {
+                        give_up(5);
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const uint32_t a0 = tc::smem_u32(sa);
+                    const uint32_t b0 = tc::smem_u32(sb + (cur.jb % NBUF) * S::b_bytes);
+#pragma unroll
+                    for (int ks = 0; ks < S::k_pad / 16; ++ks)
+                    {
+                        tc::mma_f16(tmem + acc * S::cols, tc::smem_descriptor(a0 + ks * 2 * S::lbo_a, S::lbo_a, 128),
+                                    tc::smem_descriptor(b0 + ks * 2 * S::lbo_b, S::lbo_b, 128), idesc, ks > 0);
+                    }
+                    tc::mma_commit(&bar_acc_full[acc]);
+                    tc::mma_commit(bar_a_empty);
+                    cur = cur.next(tpb);
                 }
             }
-            tc_epilogue<DC, R, OUT>(p, tmem + buf * S::cols, t, warp, lane);
-            tc::fence_before_sync();
         }
-        if (failed && tid == 0)
+        else
         {
-            // give in-flight copies and MMAs a bounded chance to land before the memory is released
-            tc::mbar_wait(&bars[1], phase_acc & 1u, p.spin_limit);
-            tc::mbar_wait(&bars[2], (phase_acc >> 1) & 1u, p.spin_limit);
+            // ------------------------------------------------ workers
+            const uint32_t row = tid & (tc_rows - 1), half = tid >> 7;
+            TcLoader<DC, R, IN, NS> loader;
+            TcCursor cur = first;
+            if constexpr (IN != tc_in_cbd)
+            {
+                if (count)
+                {
+                    loader.load(p, cur.hb / NS, cur.mt, row, half);
+                }
+            }
+            TcCursor prev = cur;
+            for (uint64_t i = 0; i <= count; ++i)
+            {
+                if (i < count)
+                {
+                    // the previous tile's MMAs no longer read the digit tile
+                    if (i > 0)
+                    {
+                        uint32_t ok = 1;
+                        if (lane == 0)
+                        {
+                            ok = tc::mbar_wait(bar_a_empty, static_cast<uint32_t>((i - 1) & 1u), p.spin_limit);
+                        }
+                        if (!__shfl_sync(0xffffffffu, ok, 0))
+                        {
+                            give_up(6);
+                            break;
+                        }
+                    }
+                    if constexpr (IN == tc_in_cbd)
+                    {
+                        tc_store_cbd(p, sa, cur.mt, row, half);
+                    }
+                    else
+                    {
+                        loader.store(sa, row, half);
+                    }
+                    tc::fence_proxy_async();
+                    mbar_arrive(bar_a_full);
+                    if constexpr (IN != tc_in_cbd)
+                    {
+                        if (i + 1 < count)
+                        {
+                            const TcCursor n1 = cur.next(tpb);
+                            loader.load(p, n1.hb / NS, n1.mt, row, half);
+                        }
+                    }
+                }
+                if (i > 0)
+                {
+                    // carry out the previous tile while the tensor core works on this one
+                    const uint32_t acc = static_cast<uint32_t>((i - 1) & 1u);
+                    uint32_t ok = 1;
+                    if (lane == 0)
+                    {
+                        ok = tc::mbar_wait(&bar_acc_full[acc], static_cast<uint32_t>(((i - 1) >> 1) & 1u),
+                                           p.spin_limit);
+                    }
+                    if (!__shfl_sync(0xffffffffu, ok, 0))
+                    {
+                        give_up(7);
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    tc_epilogue<DC, R, OUT, NS, Contig>(p, tmem + acc * S::cols, prev, warp, lane);
+                    tc::fence_before_sync();
+                    mbar_arrive(&bar_acc_empty[acc]);
+                }
+                if (*abort_flag)
+                {
+                    break;
+                }
+                prev = cur;
+                cur = cur.next(tpb);
+            }
+        }
+        __syncthreads();
+        if (*abort_flag && tid == 0)
+        {
+            // give in-flight MMAs a bounded chance to land before the memory is released
+            tc::mbar_wait(bar_a_empty, 0, p.spin_limit);
+            tc::mbar_wait(bar_a_empty, 1, p.spin_limit);
         }
         __syncthreads();
         tc::fence_after_sync();
@@ -729,14 +887,17 @@ namespace hmpc_gb300
     {
         const uint32_t* gx;      // [blocks][r][r][L]
         const uint32_t* pow256;  // [d_in][L]: 256^a * R mod q
-        uint8_t* images;         // blocks * image_bytes, zero-filled
+        uint8_t* images;         // blocks * splits images of image_bytes, zero-filled
         uint64_t blocks;
-        uint32_t r, dc, d_in, n_mma, image_bytes;
+        uint32_t r, dc, d_in, splits, n_mma, image_bytes;
         uint32_t half[8];        // floor(q / 2)
     };
 
-    // constant digits: image[h] row (k * DC + b), column (a * r + i) holds digit b
-    // of the signed value (256^a * G[k][i] mod q) in (-q/2, q/2]
+    // Constant digits: output k of block h lives in image h * splits + k / (r /
+    // splits), row (k mod (r / splits)) * DC + b, column a * r + i: balanced
+    // digit b in [-128, 127] of the signed value V = (256^a * G[k][i] mod q)
+    // in (-q/2, q/2] (V taken in two's complement; the 4L balanced digits of
+    // any |V| <= 0x7F7F..7F are exact).
     template<int L>
     __global__ void tc_expand_kernel(const TcExpandParams p, const Modulus<L> m)
     {
@@ -759,7 +920,6 @@ namespace hmpc_gb300
             pw[j] = p.pow256[a * L + j];
         }
         mont_mul<L>(w, gkx, pw, m);
-        // signed representative
         bool neg = false;
         for (int j = L - 1; j >= 0; --j)
         {
@@ -771,19 +931,22 @@ namespace hmpc_gb300
         }
         if (neg)
         {
+            // V = W - q in two's complement over L words
             uint32_t b = 0;
             for (int j = 0; j < L; ++j)
             {
-                const unsigned long long s = static_cast<unsigned long long>(m.q[j]) - w[j] - b;
+                const unsigned long long s = static_cast<unsigned long long>(w[j]) - m.q[j] - b;
                 w[j] = static_cast<uint32_t>(s);
                 b = static_cast<uint32_t>(s >> 63);
             }
         }
-        uint8_t* img = p.images + h * p.image_bytes;
+        const uint32_t outputs = p.r / p.splits;
+        uint8_t* img = p.images + (h * p.splits + k / outputs) * p.image_bytes;
+        const uint32_t k_local = k % outputs;
         int carry = 0;
         for (uint32_t b = 0; b < p.dc; ++b)
         {
-            int byte = static_cast<int>((w[b / 4] >> (8 * (b % 4))) & 255u) + carry;
+            const int byte = static_cast<int>((w[b / 4] >> (8 * (b % 4))) & 255u) + carry;
             int digit = byte;
             carry = 0;
             if (byte >= 128)
@@ -791,11 +954,7 @@ namespace hmpc_gb300
                 digit = byte - 256;
                 carry = 1;
             }
-            if (neg)
-            {
-                digit = -digit;
-            }
-            *reinterpret_cast<__half*>(img + tc::operand_offset(k * p.dc + b, a * p.r + i, p.n_mma)) =
+            *reinterpret_cast<__half*>(img + tc::operand_offset(k_local * p.dc + b, a * p.r + i, p.n_mma)) =
                 __int2half_rn(digit);
         }
     }
