@@ -157,7 +157,7 @@ namespace hmpc_gb300::detail
             // tensor-core engine; calls it does not cover run the default CUDA-core tiles
             if (tc_applicable(mod, log_n, kind, poly_rng))
             {
-                return run_tc_transform(ctx, mod, n, batch, inverse, kind, vx2, src, out);
+                return run_tc_transform(ctx, mod, n, batch, inverse, kind, vx2, src, out, choice.local_bits);
             }
             choice = hmpc_modulus::TileChoice{};
         }
@@ -654,6 +654,10 @@ int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inv
     }
     if (radix_bits == 0)
     {
+        if (local_bits < 0 || local_bits > 2)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "the tensor-core engine splits its contiguous group 1 or 2 ways");
+        }
         if (!tc_supported(mod))
         {
             return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core transform needs a 2-, 4- or 8-limb modulus below "
@@ -738,13 +742,17 @@ int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse
     };
     if (log_n >= 4 && tc_supported(mod))
     {
-        hmpc_modulus::TileChoice tensor;
-        tensor.radix_bits = 0;
-        const float sample = time_choice(tensor);
-        if (sample < best)
+        for (int splits : {1, 2})
         {
-            best = sample;
-            best_choice = tensor;
+            hmpc_modulus::TileChoice tensor;
+            tensor.radix_bits = 0;
+            tensor.local_bits = splits;
+            const float sample = time_choice(tensor);
+            if (sample < best)
+            {
+                best = sample;
+                best_choice = tensor;
+            }
         }
     }
     for (int R : {3, 2})

@@ -136,8 +136,8 @@ struct hmpc_modulus
     const hmpc_gb300::KernelTable* kt = nullptr;
     uint32_t* small_table = nullptr;  // Montgomery forms of 0..64, element-major
     std::map<uint64_t, hmpc_gb300::detail::Tables> tables;
-    // tensor-core transform constants per (log2 N, inverse)
-    std::map<std::pair<int, int>, hmpc_gb300::detail::TcTables> tc_tables;
+    // tensor-core transform constants per (log2 N, inverse, splits of the contiguous group)
+    std::map<std::tuple<int, int, int>, hmpc_gb300::detail::TcTables> tc_tables;
 
     ~hmpc_modulus()
     {
@@ -155,7 +155,9 @@ struct hmpc_modulus
     }
 
     // tile shape per (log2 N, inverse, batch): register radix bits, tile
-    // bits, column bits -- set by hmpc_modulus_tune / hmpc_modulus_set_plan
+    // bits, column bits -- set by hmpc_modulus_tune / hmpc_modulus_set_plan.
+    // Radix bits 0 selects the tensor-core engine; its local_bits is the output
+    // split (1 or 2; 0 = 1) of the group whose rows are contiguous.
     struct TileChoice
     {
         int radix_bits = 3;
@@ -215,6 +217,7 @@ namespace hmpc_gb300::detail
     // coefficients; no per-polynomial RNG)
     bool tc_supported(const hmpc_modulus* mod);
     bool tc_applicable(const hmpc_modulus* mod, int log_n, int kind, const uint32_t* poly_rng);
+    // splits: output split of the group whose rows are contiguous (1 or 2)
     int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
-                         uint32_t vx2, const uint32_t* src, uint32_t* out);
+                         uint32_t vx2, const uint32_t* src, uint32_t* out, int splits);
 }

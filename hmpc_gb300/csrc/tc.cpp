@@ -22,7 +22,7 @@ namespace
     // groups of three stages from the first stage on; the remainder (1-3
     // stages) is the last group, whose constants are the most numerous in the
     // forward direction (one matrix per block above it)
-    std::vector<TcGroupPlan> plan_groups(const TcKernels* k, int log_n, bool inverse)
+    std::vector<TcGroupPlan> plan_groups(const TcKernels* k, int log_n, bool inverse, int contiguous_splits)
     {
         const int count = (log_n + 2) / 3;
         std::vector<TcGroupPlan> groups;
@@ -37,9 +37,10 @@ namespace
             gp.out_kind = j + 1 == count ? tc_out_limbs : tc_out_digits;
             // a group with one block per 2^g contiguous elements (the forward
             // transform's last, the inverse's first) has as many constant
-            // matrices as rows per matrix are few: split each over two images
-            // so that two of them fit in shared memory and stream back to back
-            const int splits = (gp.g == 3 && gp.lo == 0) ? 2 : 1;
+            // matrices as rows per matrix are few: split in two, each image fits
+            // twice in shared memory and the next block's streams in meanwhile;
+            // unsplit, the digit tile is converted once per block instead of twice
+            const int splits = (gp.g == 3 && gp.lo == 0) ? contiguous_splits : 1;
             k->shape(1 << gp.g, gp.in_kind, gp.out_kind, splits, gp.shape);
             groups.push_back(gp);
         }
@@ -82,7 +83,8 @@ namespace
         return HMPC_OK;
     }
 
-    int prepare_tc(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, bool need_cbd, TcTables** out)
+    int prepare_tc(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, int splits, bool need_cbd,
+                   TcTables** out)
     {
         Tables* t = nullptr;
         if (int rc = mod->prepare(n, &t))
@@ -93,7 +95,7 @@ namespace
         const TcKernels* k = kernels_of(mod);
         const int L = mod->c.limbs;
         std::lock_guard<std::mutex> lock(mod->tables_mutex);
-        auto key = std::make_pair(log_n, inverse ? 1 : 0);
+        auto key = std::make_tuple(log_n, inverse ? 1 : 0, splits);
         auto it = mod->tc_tables.find(key);
         const bool fresh = it == mod->tc_tables.end();
         if (!fresh && (!need_cbd || it->second.first_cbd))
@@ -108,7 +110,7 @@ namespace
         }
         else
         {
-            tt.groups = plan_groups(k, log_n, inverse);
+            tt.groups = plan_groups(k, log_n, inverse, splits);
             size_t bytes = 0;
             for (auto& gp : tt.groups)
             {
@@ -230,7 +232,7 @@ namespace hmpc_gb300::detail
     }
 
     int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
-                         uint32_t vx2, const uint32_t* src, uint32_t* out)
+                         uint32_t vx2, const uint32_t* src, uint32_t* out, int splits)
     {
         const bool cbd = kind == producer_cbd;
         if (cbd && (vx2 < 1 || vx2 > 64))
@@ -238,7 +240,11 @@ namespace hmpc_gb300::detail
             return fail(HMPC_ERROR_UNSUPPORTED, "centred binomial needs 1 <= 2V <= 64");
         }
         TcTables* tt = nullptr;
-        if (int rc = prepare_tc(ctx, mod, n, inverse, cbd, &tt))
+        if (splits != 1 && splits != 2)
+        {
+            splits = 1;
+        }
+        if (int rc = prepare_tc(ctx, mod, n, inverse, splits, cbd, &tt))
         {
             return rc;
         }

@@ -80,12 +80,14 @@ namespace hmpc_gb300
             {
                 if (in_kind == tc_in_limbs && splits == 1 && !contig) return f.template run<8, tc_in_limbs, tc_out_digits, 1, false>();
                 if (in_kind == tc_in_limbs && splits == 2 && contig) return f.template run<8, tc_in_limbs, tc_out_digits, 2, true>();
+                if (in_kind == tc_in_limbs && splits == 1 && contig) return f.template run<8, tc_in_limbs, tc_out_digits, 1, true>();
                 if (in_kind == tc_in_cbd && splits == 1 && !contig) return f.template run<8, tc_in_cbd, tc_out_digits, 1, false>();
                 if (in_kind == tc_in_digits && splits == 1 && !contig) return f.template run<8, tc_in_digits, tc_out_digits, 1, false>();
             }
             if (out_kind == tc_out_limbs && in_kind == tc_in_digits)
             {
-                if (r == 8 && splits == 1 && !contig) return f.template run<8, tc_in_digits, tc_out_limbs, 1, false>();
+                if (r == 8 && splits == 1) return contig ? f.template run<8, tc_in_digits, tc_out_limbs, 1, true>()
+                                                         : f.template run<8, tc_in_digits, tc_out_limbs, 1, false>();
                 if (r == 8 && splits == 2 && contig) return f.template run<8, tc_in_digits, tc_out_limbs, 2, true>();
                 if (r == 4 && splits == 1) return contig ? f.template run<4, tc_in_digits, tc_out_limbs, 1, true>()
                                                          : f.template run<4, tc_in_digits, tc_out_limbs, 1, false>();

@@ -95,7 +95,8 @@ int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root
  * bits (coalescing width) -- or radix bits 0: the tensor-core engine (exact
  * fp16 MMAs over 8-bit digits, 2-, 4- and 8-limb moduli below
  * 0.996 * 2^(32L); tensor and CBD(V) producers; other calls of that shape
- * run the default tiles).  No counterpart in the reference (its transform
+ * run the default tiles), whose local_bits selects the output split (1 or 2,
+ * 0 = 1) of the group with contiguous rows.  No counterpart in the reference (its transform
  * has one schedule).  hmpc_modulus_tune times the candidates on the device
  * (scratch buffers, values irrelevant to the cost) and keeps the fastest. */
 int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits, int local_bits,

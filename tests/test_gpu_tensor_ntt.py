@@ -102,6 +102,24 @@ def test_full_size_bgv_transform(queue, oracle, cpu_threads):
     assert (z.data == big.data).all().item()
 
 
+@pytest.mark.parametrize("q", [Q_256, P_64])
+@pytest.mark.parametrize("n,batch", [(64, 5), (1 << 12, 130)])
+def test_unsplit_contiguous_group(queue, oracle, q, n, batch, cpu_threads):
+    """the forward transform's last group and the inverse's first with one
+    constant image per block (local bits 1) instead of two"""
+    om = oracle.Modulus(q)
+    gm = queue.modulus(q)
+    for inverse in (False, True):
+        gm.set_plan(n, batch, inverse, radix_bits=0, local_bits=1)
+        assert gm.plan(n, batch, inverse) == {"radix_bits": 0, "local_bits": 1, "col_bits": 4}
+    x = random_residues(oracle, om, n * batch, 3 * n + batch)
+    y = queue.ntt(Tensor.from_numpy(gm, x, (batch,), n))
+    assert np.array_equal(y.numpy(), oracle.ntt(om, n, batch, src=x, threads=cpu_threads))
+    assert np.array_equal(queue.intt(y).numpy(), x)
+    with pytest.raises(_lib.HmpcError):
+        gm.set_plan(n, batch, False, radix_bits=0, local_bits=3)
+
+
 def test_in_place_and_zero(queue, oracle):
     om = oracle.Modulus(Q_256)
     gm = queue.modulus(Q_256)
