@@ -47,10 +47,8 @@ CONFIG = {
     "l2": "per-step working set 640 MiB (messages 64 MiB + ciphertexts 512 MiB + intermediates) > 129 MB L2",
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
-# kernel: mean of the four launches of two fused CBD(10) transforms of 160
-# polynomials (194.3 MB), scaled by 256/160 to this batch
-# (profiles/ntt_pass_kernel_cbd_traffic_n32768_L8.md)
-DOMINANT_TRAFFIC_BYTES = 310.8e6
+# kernel (tc_group_kernel) from an ncu capture; None until captured
+DOMINANT_TRAFFIC_BYTES = None
 
 
 def mont_mul_ops(limbs):
@@ -200,6 +198,75 @@ def hbm_peak_gbs():
         return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+def bf16_peak_tflops():
+    """measured dense bf16 (= fp16) tensor rate of the GB300s, burst"""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+def dominant_roofline(q, transform_ms, per_transform, int_peak):
+    """Roofline of the transform kernel that dominates a step (the fused
+    CBD(10) -> NTT of the batch).  Tensor-core engine: algorithmic DRAM bytes
+    and fp16 MMA flops per launch from the engine's own cost model, against
+    the measured HBM copy rate and dense bf16 rate; the bound is the larger
+    fraction.  CUDA-core tiles: 32-bit multiplies of the Montgomery products
+    against the live integer-multiply probe."""
+    from hmpc_gb300 import _lib
+
+    plan = q.plan(N, BATCH)
+    launch_ms = transform_ms / per_transform
+    launch_s = launch_ms * 1e-3
+    hbm, hbm_src = hbm_peak_gbs()
+    if plan["radix_bits"] == 0:
+        cost = q.tc_cost(N, BATCH, producer=_lib.PRODUCER_CBD, splits=plan["local_bits"] or 1)
+        bytes_per_launch = cost["bytes"] / cost["launches"]
+        flops_per_launch = cost["flops"] / cost["launches"]
+        gbs = bytes_per_launch / launch_s / 1e9
+        tflops = flops_per_launch / launch_s / 1e12
+        tensor_peak, tensor_src = bf16_peak_tflops()
+        hbm_view = {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                    "algorithmic_bytes_per_launch": bytes_per_launch, "peak_source": hbm_src}
+        tensor_view = {"achieved": tflops, "peak": tensor_peak, "unit": "TFLOP/s", "frac": tflops / tensor_peak,
+                       "mma_flops_per_launch": flops_per_launch,
+                       "peak_source": tensor_src + " (dense bf16; fp16 MMAs run at the same rate)"}
+        primary, other, bound = ((hbm_view, tensor_view, "hbm") if hbm_view["frac"] >= tensor_view["frac"]
+                                 else (tensor_view, hbm_view, "tensor"))
+        return {
+            "bound": bound,
+            "kernel": "tc_group_kernel (tensor-core transform groups: fused CBD(10) sampler -> NTT, 256 x N=2^15, L=8)",
+            "achieved": primary["achieved"],
+            "peak": primary["peak"],
+            "unit": primary["unit"],
+            "frac": primary["frac"],
+            "traffic": DOMINANT_TRAFFIC_BYTES,
+            "peak_source": primary["peak_source"],
+            "hbm_view" if bound == "tensor" else "tensor_view": other,
+            "launches_per_transform": per_transform,
+            "launch_ms": launch_ms,
+            "plan": plan,
+        }
+    butterflies = BATCH * (N // 2) * (N.bit_length() - 1)
+    ops_per_launch = butterflies * mont_mul_ops(q.limbs) / per_transform
+    achieved = ops_per_launch / launch_s
+    algorithmic_bytes = 3 * BATCH * N * q.limbs * 4 / per_transform
+    return {
+        "bound": "int",
+        "kernel": "ntt_pass_kernel (fused CBD(10) sampler -> NTT, 256 x N=2^15, L=8)",
+        "achieved": achieved / 1e12,
+        "peak": int_peak / 1e12,
+        "unit": "T int32-mul/s",
+        "frac": achieved / int_peak,
+        "traffic": None,
+        "peak_source": "measured live: hmpc_probe_int_multiply_rate (independent mad.lo/mad.hi chains)",
+        "hbm_view": {"achieved": algorithmic_bytes / launch_s / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": algorithmic_bytes / launch_s / 1e9 / hbm, "peak_source": hbm_src},
+        "launch_ms": launch_ms,
+        "plan": plan,
+    }
 
 
 def secondary_metrics(queue, int_peak):
@@ -380,8 +447,10 @@ def main():
     q, p = queue.modulus(Q_256), queue.modulus(P_64)
     q.prepare(N)
     p.prepare(N)
-    # autotune the tile shape of the batch's transforms (kept per modulus)
+    # autotune the tile shape (or engine) of the batch's transforms (kept per
+    # modulus): the forward transforms mod q, the inverse one mod p
     q.tune(N, BATCH)
+    p.tune(N, BATCH, inverse=True)
     queue.nonce = [0, 0, 0]
     s0, key0 = lhe.keygen(queue, q, p, N)
     msgs = queue.uniform(p, (BATCH,), N)
@@ -444,7 +513,7 @@ def main():
     ok = bool((lhe.dec(queue, s, back, p).data == msgs.data).all().item())
 
     # ------------------------------------------- dominant kernel roofline
-    # the fused CBD(10) -> NTT over the batch: ntt_pass_kernel launches
+    # the fused CBD(10) -> NTT over the batch: the transform's kernel launches
     reps = 5
     before = queue.launches
     queue.ntt_centered_binomial(q, N, (BATCH,), 20, out=ct.c1)
@@ -457,13 +526,8 @@ def main():
     k_stop.record(stream)
     barrier()
     transform_ms = k_start.elapsed_time(k_stop) / reps
-    launch_ms = transform_ms / per_transform
-    butterflies = BATCH * (N // 2) * (N.bit_length() - 1)
-    ops_per_launch = butterflies * mont_mul_ops(q.limbs) / per_transform
-    achieved = ops_per_launch / (launch_ms * 1e-3)
-    # the batch is written once by pass A and read + written once by pass B
-    algorithmic_bytes = 3 * BATCH * N * q.limbs * 4 / per_transform
     peak = queue.int_multiply_rate()
+    roofline = dominant_roofline(q, transform_ms, per_transform, peak)
 
     if rank == 0:
         line = {
@@ -488,26 +552,7 @@ def main():
                 "decrypts_ok": ok,
             },
             "gpu_launches": launches,
-            "roofline": {
-                "bound": "int",
-                "kernel": "ntt_pass_kernel (fused CBD(10) sampler -> NTT, 256 x N=2^15, L=8)",
-                "achieved": achieved / 1e12,
-                "peak": peak / 1e12,
-                "unit": "T int32-mul/s",
-                "frac": achieved / peak,
-                "traffic": DOMINANT_TRAFFIC_BYTES,
-                "peak_source": "measured live: hmpc_probe_int_multiply_rate (independent mad.lo/mad.hi chains)",
-                "ops_per_launch": ops_per_launch,
-                "tile": q.plan(N, BATCH),
-                "hbm_view": {
-                    "algorithmic_bytes_per_launch": algorithmic_bytes,
-                    "achieved_gbs": algorithmic_bytes / (launch_ms * 1e-3) / 1e9,
-                    "peak_gbs": hbm_peak_gbs()[0],
-                    "frac": algorithmic_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak_gbs()[0],
-                    "peak_source": hbm_peak_gbs()[1],
-                },
-                "launch_ms": launch_ms,
-            },
+            "roofline": roofline,
             "clocks": clocks.summary(),
         }
         if not args.no_cpu_baseline:

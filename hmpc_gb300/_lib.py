@@ -31,6 +31,10 @@ class HmpcError(RuntimeError):
         self.code = code
 
 
+class TcCost(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_uint32), ("bytes", ctypes.c_double), ("flops", ctypes.c_double)]
+
+
 class Producer(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int),
@@ -63,6 +67,7 @@ SIGNATURES = {
     "hmpc_modulus_root": ([_vp, _u64, _int, _u32p], _int),
     "hmpc_modulus_set_plan": ([_vp, _u64, _u64, _int, _int, _int, _int], _int),
     "hmpc_modulus_get_plan": ([_vp, _u64, _u64, _int] + [ctypes.POINTER(_int)] * 3, _int),
+    "hmpc_modulus_tc_cost": ([_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(TcCost)], _int),
     "hmpc_modulus_tune": ([_vp, _u64, _u64, _int, ctypes.POINTER(ctypes.c_float)], _int),
     "hmpc_modulus_twiddles": ([_vp, _u64, _int, _u32p], _int),
     "hmpc_tensor_alloc": ([_vp, _u64, ctypes.POINTER(_vp)], _int),

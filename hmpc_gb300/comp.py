@@ -67,6 +67,12 @@ class Modulus:
                   ctypes.byref(cb))
         return {"radix_bits": r.value, "local_bits": lb.value, "col_bits": cb.value}
 
+    def tc_cost(self, n, batch, inverse=False, producer=_lib.PRODUCER_TENSOR, splits=1):
+        """launches, algorithmic DRAM bytes and MMA flops of one tensor-core transform"""
+        out = _lib.TcCost()
+        _lib.call("hmpc_modulus_tc_cost", self.handle, n, batch, int(inverse), producer, splits, ctypes.byref(out))
+        return {"launches": out.launches, "bytes": out.bytes, "flops": out.flops}
+
     def root(self, n, inverse=False):
         out = (ctypes.c_uint32 * 16)()
         _lib.call("hmpc_modulus_root", self.handle, n, int(inverse), out)

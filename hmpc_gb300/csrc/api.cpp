@@ -641,6 +641,20 @@ int hmpc_modulus_get_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inv
     return HMPC_OK;
 }
 
+int hmpc_modulus_tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int producer_kind, int splits,
+                         hmpc_tc_cost* out)
+{
+    if (!mod || !out)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    return tc_cost(mod, n, batch, inverse != 0, producer_kind, splits, out);
+}
+
 int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits,
                           int local_bits, int col_bits)
 {

@@ -220,4 +220,5 @@ namespace hmpc_gb300::detail
     // splits: output split of the group whose rows are contiguous (1 or 2)
     int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                          uint32_t vx2, const uint32_t* src, uint32_t* out, int splits);
+    int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out);
 }

@@ -317,4 +317,39 @@ namespace hmpc_gb300::detail
         }
         return HMPC_OK;
     }
+
+    int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out)
+    {
+        if (!tc_supported(mod) || n < 16 || (kind != producer_tensor && kind != producer_cbd) ||
+            (kind == producer_cbd && inverse) || (splits != 1 && splits != 2))
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core engine does not cover this transform");
+        }
+        const TcKernels* k = kernels_of(mod);
+        const int log_n = __builtin_ctzll(n);
+        const std::vector<TcGroupPlan> groups = plan_groups(k, log_n, inverse, splits);
+        const double elements = static_cast<double>(n) * static_cast<double>(batch);
+        const double limb_bytes = 4.0 * mod->c.limbs;
+        out->launches = static_cast<uint32_t>(groups.size());
+        out->bytes = 0.0;
+        out->flops = 0.0;
+        for (size_t j = 0; j < groups.size(); ++j)
+        {
+            TcShapeInfo shape = groups[j].shape;
+            const bool cbd = j == 0 && kind == producer_cbd;
+            if (cbd)
+            {
+                k->shape(8, tc_in_cbd, tc_out_digits, 1, shape);
+            }
+            const double in = j == 0 ? (cbd ? 0.0 : limb_bytes) : 4.0 * shape.w_in;
+            const double outb = j + 1 == groups.size() ? limb_bytes : 4.0 * shape.w_out;
+            const uint64_t rows = batch << groups[j].lo;
+            const double tiles = static_cast<double>(groups[j].blocks * shape.splits) *
+                                 static_cast<double>((rows + tc_rows - 1) / tc_rows);
+            out->bytes += elements * (in + outb) + static_cast<double>(groups[j].blocks * shape.splits) * shape.b_bytes;
+            out->flops += tiles * 2.0 * tc_rows * shape.n_mma * shape.k_pad;
+        }
+        return HMPC_OK;
+    }
 }
+

@@ -53,7 +53,7 @@ namespace hmpc_gb300
             {
                 return configured;
             }
-            tc_group_kernel<DC, R, IN, OUT, NS, Contig><<<grid, tc_threads + 32, smem, stream>>>(p);
+            tc_group_kernel<DC, R, IN, OUT, NS, Contig><<<grid, tc_workers<Contig> + 32, smem, stream>>>(p);
             return cudaGetLastError();
         }
 

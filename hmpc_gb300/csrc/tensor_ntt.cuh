@@ -65,7 +65,11 @@ namespace hmpc_gb300
     };
 
     constexpr int tc_rows = 128;
-    constexpr int tc_threads = 256;
+    // worker threads of a group kernel: 16 warps, or 8 where a tile row's
+    // elements are adjacent (wider output runs per thread)
+    template<bool Contig>
+    constexpr int tc_workers = Contig ? 256 : 512;
+    constexpr int tc_max_threads = 512 + 32;
 
     struct TcGroupParams
     {
@@ -176,16 +180,18 @@ namespace hmpc_gb300
         return r;
     }
 
-    // loader of digit / limb tiles: thread (row, half) owns words [half * WH, ...) of the row's R elements
-    template<int DC, int R, int IN, int NS>
+    // loader of digit / limb tiles: thread (row, part) owns words part, part +
+    // tc_parts, ... of the row's R elements
+    template<int DC, int R, int IN, int NS, int Parts>
     struct TcLoader
     {
         using S = TcShape<DC, R, IN, NS>;
-        static constexpr int wh = S::w_in > 0 ? (S::w_in + 1) / 2 : 1;
+        static constexpr int tc_parts = Parts;
+        static constexpr int wh = S::w_in > 0 ? (S::w_in + tc_parts - 1) / tc_parts : 1;
         uint32_t v[wh][R];
 
         __device__ __forceinline__ void load(const TcGroupParams& p, uint64_t h, uint32_t mt, uint32_t row,
-                                             uint32_t half)
+                                             uint32_t part)
         {
             const TcRow r = tc_row<S::g>(p, h, mt, row);
             const uint32_t* rp = p.in + r.base;
@@ -193,7 +199,7 @@ namespace hmpc_gb300
 #pragma unroll
             for (int wi = 0; wi < wh; ++wi)
             {
-                const uint32_t w = half * wh + wi;
+                const uint32_t w = part + tc_parts * wi;
                 const bool live = r.ok && w < static_cast<uint32_t>(S::w_in);
                 const uint32_t* wp = rp + w * p.elements;
                 if (live && contiguous)
@@ -227,13 +233,13 @@ namespace hmpc_gb300
             }
         }
 
-        __device__ __forceinline__ void store(uint8_t* sa, uint32_t row, uint32_t half) const
+        __device__ __forceinline__ void store(uint8_t* sa, uint32_t row, uint32_t part) const
         {
             constexpr int bias = IN == tc_in_digits ? 128 : 0;
 #pragma unroll
             for (int wi = 0; wi < wh; ++wi)
             {
-                const uint32_t w = half * wh + wi;
+                const uint32_t w = part + tc_parts * wi;
                 if (w >= static_cast<uint32_t>(S::w_in))
                 {
                     continue;
@@ -285,48 +291,49 @@ namespace hmpc_gb300
     // first forward group fed by centred binomial samples: r = 8, stage-0 pairs
     // (m, m + 4) of a row come from one generator with counter = poly * N +
     // index of the first element, first draw for m, second for m + 4
-    // (number_theoretic_transform.hpp:316-329, comp/queue.hpp:191-212)
+    // (number_theoretic_transform.hpp:316-329, comp/queue.hpp:191-212); thread
+    // (row, part) draws the pair m = part
+    __device__ __forceinline__ void st_shared_u16(uint8_t* p, uint16_t a)
+    {
+        asm volatile("st.shared.u16 [%0], %1;" ::"r"(tc::smem_u32(p)), "h"(a) : "memory");
+    }
+
     __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t row,
-                                                 uint32_t half)
+                                                 uint32_t part)
     {
         const TcRow r = tc_row<3>(p, 0, mt, row);
-        int e_u[2] = {0, 0}, e_v[2] = {0, 0};
+        int e_u = 0, e_v = 0;
         if (r.ok)
         {
             const int count = 2 * static_cast<int>(p.vx2);
             const int nw = static_cast<int>(p.nw);
+            const uint64_t idx = r.base + (static_cast<uint64_t>(part) << p.lo);
+            uint32_t w[8];
+            chacha_stream<8>(p.rng, static_cast<uint32_t>(idx), w);
+            int a = 0, b = 0;
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
+            for (int i = 0; i < 8; ++i)
             {
-                const uint64_t idx = r.base + (static_cast<uint64_t>(2 * half + j) << p.lo);
-                uint32_t w[8];
-                chacha_stream<8>(p.rng, static_cast<uint32_t>(idx), w);
-                int a = 0, b = 0;
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
+                const int iv = i - nw;  // word of the second sample
+                uint32_t mu = 0u, mv = 0u;
+                if (i < nw)
                 {
-                    const int iv = i - nw;  // word of the second sample
-                    uint32_t mu = 0u, mv = 0u;
-                    if (i < nw)
-                    {
-                        mu = (i == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
-                    }
-                    else if (iv < nw)
-                    {
-                        mv = (iv == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
-                    }
-                    a += __popc(w[i] & mu);
-                    b += __popc(w[i] & mv);
+                    mu = (i == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
                 }
-                e_u[j] = a - static_cast<int>(p.vx2);
-                e_v[j] = b - static_cast<int>(p.vx2);
+                else if (iv < nw)
+                {
+                    mv = (iv == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
+                }
+                a += __popc(w[i] & mu);
+                b += __popc(w[i] & mv);
             }
+            e_u = a - static_cast<int>(p.vx2);
+            e_v = b - static_cast<int>(p.vx2);
         }
         uint8_t* seg = sa + tc::operand_offset(row, 0, tc_rows);
-        __half2 lo = __halves2half2(__int2half_rn(e_u[0]), __int2half_rn(e_u[1]));
-        __half2 hi = __halves2half2(__int2half_rn(e_v[0]), __int2half_rn(e_v[1]));
-        st_shared_u32(seg + 4 * half, *reinterpret_cast<uint32_t*>(&lo));
-        st_shared_u32(seg + 8 + 4 * half, *reinterpret_cast<uint32_t*>(&hi));
+        const __half hu = __int2half_rn(e_u), hv = __int2half_rn(e_v);
+        st_shared_u16(seg + 2 * part, *reinterpret_cast<const uint16_t*>(&hu));
+        st_shared_u16(seg + 8 + 2 * part, *reinterpret_cast<const uint16_t*>(&hv));
     }
 
     __device__ __forceinline__ uint32_t pack_bytes(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3)
@@ -438,7 +445,7 @@ namespace hmpc_gb300
     }
 
     // carry the accumulator of one tile out of TMEM: each thread owns one row
-    // and Per consecutive output elements of the block's split; Contig: the
+    // and `per` consecutive output elements of the block's split; Contig: the
     // row's elements are adjacent (no column bits), stored as vectors
     template<int DC, int R, int OUT, int NS, bool Contig>
     __device__ __forceinline__ void tc_epilogue(const TcGroupParams& p, uint32_t tmem, const TcCursor& cur,
@@ -448,8 +455,13 @@ namespace hmpc_gb300
         constexpr int L = DC / 4;
         constexpr int W = (DC + 2 + 3) / 4;
         constexpr int outputs = R / NS;
-        constexpr int per = outputs / 2;
+        constexpr int kgroups = tc_workers<Contig> / tc_rows;  // warps sharing a TMEM lane quadrant
+        constexpr int per = outputs >= kgroups ? outputs / kgroups : 1;
         constexpr int words_out = OUT == tc_out_digits ? W : L;
+        if ((warp >> 2) * per >= static_cast<uint32_t>(outputs))
+        {
+            return;  // more warps than output elements (R = 2)
+        }
         const uint32_t lg = warp & 3u;
         const uint32_t row = 32u * lg + lane;
         const uint64_t h = cur.hb / NS;
@@ -539,30 +551,33 @@ namespace hmpc_gb300
     }
 
     // One CTA per SM, persistent over a contiguous range of tiles, warp-specialised:
-    // warps 0-7 convert each 128-row digit tile into shared memory and carry
-    // accumulators out of TMEM; one thread of warp 8 streams the constant
+    // warps 0-15 convert each 128-row digit tile into shared memory and carry
+    // accumulators out of TMEM; one thread of warp 16 streams the constant
     // operands (bulk copies) and issues the MMAs.  mbarriers hand over the
-    // digit tile (full: 256 arrivals; empty: MMA commit), the two TMEM
-    // accumulators (full: MMA commit; empty: 256 arrivals) and the constant
+    // digit tile (full: 512 arrivals; empty: MMA commit), the two TMEM
+    // accumulators (full: MMA commit; empty: 512 arrivals) and the constant
     // buffers (transaction count).  Every wait is bounded; a timeout sets the
     // error word and both sides leave their loops.
     template<int DC, int R, int IN, int OUT, int NS, bool Contig>
-    __global__ void __launch_bounds__(tc_threads + 32, 1) tc_group_kernel(const TcGroupParams p)
+    __global__ void __launch_bounds__(tc_workers<Contig> + 32, 1) tc_group_kernel(const TcGroupParams p)
     {
         using S = TcShape<DC, R, IN, NS>;
+        constexpr int tc_threads = tc_workers<Contig>;
+        static_assert(IN != tc_in_cbd || tc_threads / tc_rows == 4, "the CBD loader draws one pair per thread");
         constexpr int NBUF = S::nbuf;
         extern __shared__ __align__(1024) uint8_t tc_smem[];
         uint8_t* sb = tc_smem;                           // NBUF constant buffers
         uint8_t* sa = tc_smem + NBUF * S::b_bytes;       // the digit tile
         uint64_t* bars = reinterpret_cast<uint64_t*>(sa + S::a_bytes);
         uint64_t* bar_b = bars;           // [2] constants full
-        uint64_t* bar_a_full = bars + 2;  // digit tile stored (256 arrivals)
+        uint64_t* bar_a_full = bars + 2;  // digit tile stored (one arrival per worker)
         uint64_t* bar_a_empty = bars + 3; // MMAs of the tile complete (commit)
         uint64_t* bar_acc_full = bars + 4;   // [2] accumulator ready (commit)
-        uint64_t* bar_acc_empty = bars + 6;  // [2] accumulator read out (256 arrivals)
-        uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+        uint64_t* bar_acc_empty = bars + 6;  // [2] accumulator read out (one arrival per worker)
+        uint64_t* bar_k0 = bars + 8;         // MMAs on the first K half complete (commit)
+        uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
         volatile uint32_t* abort_flag = tslot + 1;
-        static_assert(8 * sizeof(uint64_t) + 2 * sizeof(uint32_t) <= S::control_bytes, "control block");
+        static_assert(9 * sizeof(uint64_t) + 2 * sizeof(uint32_t) <= S::control_bytes, "control block");
 
         const uint32_t tid = threadIdx.x;
         const uint32_t warp = tid >> 5, lane = tid & 31u;
@@ -595,6 +610,7 @@ namespace hmpc_gb300
             tc::mbar_init(&bar_acc_full[1], 1);
             tc::mbar_init(&bar_acc_empty[0], tc_threads);
             tc::mbar_init(&bar_acc_empty[1], tc_threads);
+            tc::mbar_init(bar_k0, 1);
             *abort_flag = 0;
             tc::mbar_init_fence();
         }
@@ -616,46 +632,71 @@ namespace hmpc_gb300
         if (warp == tc_threads / 32)
         {
             // ------------------------------------------------ MMA and copies
+            // Two constant buffers (NBUF 2): block jb's image goes to buffer jb % 2
+            // as soon as block jb - 2's MMAs are complete.  One buffer (NBUF 1): the
+            // image arrives in two K halves on their own barriers, the first as
+            // soon as the previous block's MMAs on the first half completed, so the
+            // next block's constants stream in while the last tile finishes.
             if (lane == 0 && count)
             {
                 constexpr uint32_t idesc = tc::f16_instr_descriptor(tc_rows, S::n_mma);
-                auto issue_b = [&](uint32_t jb) {
-                    const uint32_t buf = jb % NBUF;
-                    tc::mbar_arrive_expect_tx(&bar_b[buf], S::b_bytes);
-                    tc::bulk_g2s(sb + buf * S::b_bytes, p.images + (hb_first + jb) * S::b_bytes, S::b_bytes,
-                                 &bar_b[buf]);
-                };
-                for (uint32_t j = 0; j < static_cast<uint32_t>(NBUF); ++j)
-                {
-                    if (hb_first + j <= hb_last)
+                constexpr int ks_total = S::k_pad / 16;
+                constexpr int ks_half = NBUF == 1 ? (ks_total + 1) / 2 : ks_total;
+                constexpr uint32_t h0_bytes = NBUF == 1 ? 2u * ks_half * S::lbo_b : S::b_bytes;
+                auto copy = [&](uint32_t jb, uint32_t piece) {
+                    // NBUF 2: piece = buffer (whole image); NBUF 1: piece = K half
+                    const uint8_t* src = p.images + (hb_first + jb) * S::b_bytes;
+                    if constexpr (NBUF == 2)
                     {
-                        issue_b(j);
+                        tc::mbar_arrive_expect_tx(&bar_b[piece], S::b_bytes);
+                        tc::bulk_g2s(sb + piece * S::b_bytes, src, S::b_bytes, &bar_b[piece]);
                     }
+                    else
+                    {
+                        const uint32_t off = piece ? h0_bytes : 0u;
+                        const uint32_t bytes = piece ? S::b_bytes - h0_bytes : h0_bytes;
+                        tc::mbar_arrive_expect_tx(&bar_b[piece], bytes);
+                        tc::bulk_g2s(sb + off, src + off, bytes, &bar_b[piece]);
+                    }
+                };
+                copy(0, 0);
+                if (NBUF == 1 || hb_first + 1 <= hb_last)
+                {
+                    copy(NBUF == 1 ? 0u : 1u, 1);
                 }
                 TcCursor cur = first;
                 uint32_t prev_jb = ~0u;
                 for (uint64_t i = 0; i < count && !*abort_flag; ++i)
                 {
                     const uint32_t acc = static_cast<uint32_t>(i & 1u);
-                    if (cur.jb != prev_jb)
+                    const uint32_t prev = static_cast<uint32_t>((i - 1) & 1u);
+                    const bool new_block = cur.jb != prev_jb;
+                    if (new_block && i > 0)
                     {
-                        if (i > 0 && hb_first + prev_jb + NBUF <= hb_last)
+                        if constexpr (NBUF == 1)
                         {
-                            // the previous block's buffer is free once its last MMAs completed
-                            if (!tc::mbar_wait(bar_a_empty, static_cast<uint32_t>((i - 1) & 1u), p.spin_limit))
+                            if (!tc::mbar_wait(bar_k0, prev, p.spin_limit))
                             {
                                 give_up(3);
                                 break;
                             }
-                            issue_b(prev_jb + NBUF);
+                            copy(cur.jb, 0);
+                            if (!tc::mbar_wait(bar_a_empty, prev, p.spin_limit))
+                            {
+                                give_up(3);
+                                break;
+                            }
+                            copy(cur.jb, 1);
                         }
-                        const uint32_t buf = cur.jb % NBUF;
-                        if (!tc::mbar_wait(&bar_b[buf], (cur.jb / NBUF) & 1u, p.spin_limit))
+                        else if (hb_first + prev_jb + 2 <= hb_last)
                         {
-                            give_up(1);
-                            break;
+                            if (!tc::mbar_wait(bar_a_empty, prev, p.spin_limit))
+                            {
+                                give_up(3);
+                                break;
+                            }
+                            copy(prev_jb + 2, prev_jb % 2);
                         }
-                        prev_jb = cur.jb;
                     }
                     if (!tc::mbar_wait(bar_a_full, static_cast<uint32_t>(i & 1u), p.spin_limit))
                     {
@@ -668,17 +709,42 @@ namespace hmpc_gb300
                         give_up(5);
                         break;
                     }
+                    const uint32_t piece0 = NBUF == 1 ? 0u : cur.jb % 2;
+                    const uint32_t parity = NBUF == 1 ? (cur.jb & 1u) : ((cur.jb / 2) & 1u);
+                    if (new_block && !tc::mbar_wait(&bar_b[piece0], parity, p.spin_limit))
+                    {
+                        give_up(1);
+                        break;
+                    }
                     tc::fence_after_sync();
                     const uint32_t a0 = tc::smem_u32(sa);
-                    const uint32_t b0 = tc::smem_u32(sb + (cur.jb % NBUF) * S::b_bytes);
+                    const uint32_t b0 = tc::smem_u32(sb + (NBUF == 1 ? 0u : (cur.jb % 2) * S::b_bytes));
 #pragma unroll
-                    for (int ks = 0; ks < S::k_pad / 16; ++ks)
+                    for (int ks = 0; ks < ks_half; ++ks)
                     {
                         tc::mma_f16(tmem + acc * S::cols, tc::smem_descriptor(a0 + ks * 2 * S::lbo_a, S::lbo_a, 128),
                                     tc::smem_descriptor(b0 + ks * 2 * S::lbo_b, S::lbo_b, 128), idesc, ks > 0);
                     }
+                    if constexpr (NBUF == 1)
+                    {
+                        tc::mma_commit(bar_k0);
+                        if (new_block && !tc::mbar_wait(&bar_b[1], parity, p.spin_limit))
+                        {
+                            give_up(1);
+                            break;
+                        }
+                        tc::fence_after_sync();
+#pragma unroll
+                        for (int ks = ks_half; ks < ks_total; ++ks)
+                        {
+                            tc::mma_f16(tmem + acc * S::cols,
+                                        tc::smem_descriptor(a0 + ks * 2 * S::lbo_a, S::lbo_a, 128),
+                                        tc::smem_descriptor(b0 + ks * 2 * S::lbo_b, S::lbo_b, 128), idesc, true);
+                        }
+                    }
                     tc::mma_commit(&bar_acc_full[acc]);
                     tc::mma_commit(bar_a_empty);
+                    prev_jb = cur.jb;
                     cur = cur.next(tpb);
                 }
             }
@@ -686,14 +752,14 @@ namespace hmpc_gb300
         else
         {
             // ------------------------------------------------ workers
-            const uint32_t row = tid & (tc_rows - 1), half = tid >> 7;
-            TcLoader<DC, R, IN, NS> loader;
+            const uint32_t row = tid & (tc_rows - 1), part = tid / tc_rows;
+            TcLoader<DC, R, IN, NS, tc_threads / tc_rows> loader;
             TcCursor cur = first;
             if constexpr (IN != tc_in_cbd)
             {
                 if (count)
                 {
-                    loader.load(p, cur.hb / NS, cur.mt, row, half);
+                    loader.load(p, cur.hb / NS, cur.mt, row, part);
                 }
             }
             TcCursor prev = cur;
@@ -717,11 +783,11 @@ namespace hmpc_gb300
                     }
                     if constexpr (IN == tc_in_cbd)
                     {
-                        tc_store_cbd(p, sa, cur.mt, row, half);
+                        tc_store_cbd(p, sa, cur.mt, row, part);
                     }
                     else
                     {
-                        loader.store(sa, row, half);
+                        loader.store(sa, row, part);
                     }
                     tc::fence_proxy_async();
                     mbar_arrive(bar_a_full);
@@ -730,7 +796,7 @@ namespace hmpc_gb300
                         if (i + 1 < count)
                         {
                             const TcCursor n1 = cur.next(tpb);
-                            loader.load(p, n1.hb / NS, n1.mt, row, half);
+                            loader.load(p, n1.hb / NS, n1.mt, row, part);
                         }
                     }
                 }

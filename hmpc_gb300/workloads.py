@@ -112,6 +112,12 @@ def main(argv=None):
         p = queue.modulus(MODULI["p64"])
         q.prepare(args.n)
         p.prepare(args.n)
+        if args.tune:
+            result["tuned_ms"] = q.tune(args.n, args.batch)
+            p.tune(args.n, args.batch, inverse=True)
+        elif args.radix_bits is not None:
+            q.set_plan(args.n, args.batch, False, args.radix_bits, args.local_bits, args.col_bits)
+        result["tile"] = q.plan(args.n, args.batch)
         s, key = lhe.keygen(queue, q, p, args.n)
         msgs = queue.uniform(p, (args.batch,), args.n)
         ct = lhe.Ciphertext(Tensor(q, (args.batch,), args.n), Tensor(q, (args.batch,), args.n))

@@ -107,6 +107,21 @@ int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse
  * bits 4). */
 int hmpc_modulus_get_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int* radix_bits, int* local_bits,
                           int* col_bits);
+/* Cost model of one tensor-core transform (no counterpart in the reference):
+ * kernel launches, algorithmic DRAM bytes (digit / limb planes read and
+ * written once per group, constant images read once per block) and dense
+ * fp16 MMA flops, for `batch` polynomials of degree n fed by `producer_kind`
+ * (HMPC_PRODUCER_TENSOR or HMPC_PRODUCER_CBD) with the output split
+ * `splits` (1 or 2).  HMPC_ERROR_UNSUPPORTED when the engine does not cover
+ * the modulus. */
+typedef struct hmpc_tc_cost
+{
+    uint32_t launches;
+    double bytes;
+    double flops;
+} hmpc_tc_cost;
+int hmpc_modulus_tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int producer_kind, int splits,
+                         hmpc_tc_cost* out);
 /* Copy a cached twiddle table (n*L words, element-major) to host memory. */
 int hmpc_modulus_twiddles(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* host_table);
 
