@@ -47,8 +47,10 @@ CONFIG = {
     "l2": "per-step working set 640 MiB (messages 64 MiB + ciphertexts 512 MiB + intermediates) > 129 MB L2",
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
-# kernel (tc_group_kernel) from an ncu capture; None until captured
-DOMINANT_TRAFFIC_BYTES = None
+# kernel: mean over the five tc_group_kernel launches of one fused CBD(10)
+# transform of 256 x 2^15 (one-pass metrics captured at this size;
+# profiles/tc_group_kernel_cbd_n32768_L8_traffic.md)
+DOMINANT_TRAFFIC_BYTES = 711.9e6
 
 
 def mont_mul_ops(limbs):

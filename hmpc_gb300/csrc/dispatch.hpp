@@ -91,8 +91,9 @@ namespace hmpc_gb300
     struct TcKernels
     {
         int digits;
-        cudaError_t (*group)(const TcGroupParams& p, int r, int in_kind, int out_kind, int splits, unsigned grid,
-                             cudaStream_t stream);
+        // layout bit 0: the input digit planes are blocked per row, bit 1: the output
+        cudaError_t (*group)(const TcGroupParams& p, int r, int in_kind, int out_kind, int splits, int layout,
+                             unsigned grid, cudaStream_t stream);
         bool (*shape)(int r, int in_kind, int out_kind, int splits, TcShapeInfo& out);
         cudaError_t (*gen)(const TcGenParams& p, const HostModulus& m, cudaStream_t stream);
         cudaError_t (*expand)(const TcExpandParams& p, const HostModulus& m, cudaStream_t stream);

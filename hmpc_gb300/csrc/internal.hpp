@@ -37,6 +37,7 @@ namespace hmpc_gb300::detail
         uint32_t s0 = 0, g = 0, lo = 0;
         uint64_t blocks = 0;
         int in_kind = 0, out_kind = 0;
+        int layout = 0;  // bit 0: reads digit planes blocked per row, bit 1: writes them
         TcShapeInfo shape;
         size_t offset = 0;
     };

@@ -44,6 +44,15 @@ namespace
             k->shape(1 << gp.g, gp.in_kind, gp.out_kind, splits, gp.shape);
             groups.push_back(gp);
         }
+        // a last group whose rows are adjacent elements reads digit planes
+        // blocked per row (one contiguous run per row instead of a short piece
+        // per word plane), written so by the group before it
+        TcGroupPlan& last = groups.back();
+        if (last.lo == 0 && last.shape.splits == 1 && last.in_kind == tc_in_digits && groups.size() >= 2)
+        {
+            last.layout |= 1;
+            groups[groups.size() - 2].layout |= 2;
+        }
         return groups;
     }
 
@@ -300,11 +309,12 @@ namespace hmpc_gb300::detail
                 p.q[i] = mod->c.q[static_cast<size_t>(i)];
             }
             p.inv_q_top = inv_q_top;
+            p.block_shift = tt->groups.back().g;  // the last group's elements per row
             const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
             const int in_kind = j == 0 ? (cbd ? static_cast<int>(tc_in_cbd) : static_cast<int>(tc_in_limbs))
                                        : static_cast<int>(tc_in_digits);
             const int splits = (j == 0 && cbd) ? 1 : static_cast<int>(gp.shape.splits);
-            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, grid, ctx->stream);
+            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, gp.layout, grid, ctx->stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching a tensor-core transform group");

@@ -36,7 +36,7 @@ namespace hmpc_gb300
             return m;
         }
 
-        template<int R, int IN, int OUT, int NS, bool Contig>
+        template<int R, int IN, int OUT, int NS, bool Contig, int Lay>
         cudaError_t launch(const TcGroupParams& p, unsigned grid, cudaStream_t stream)
         {
             using S = TcShape<DC, R, IN, NS>;
@@ -46,14 +46,14 @@ namespace hmpc_gb300
             static std::once_flag once;
             static cudaError_t configured = cudaSuccess;
             std::call_once(once, [] {
-                configured = cudaFuncSetAttribute(tc_group_kernel<DC, R, IN, OUT, NS, Contig>,
+                configured = cudaFuncSetAttribute(tc_group_kernel<DC, R, IN, OUT, NS, Contig, Lay>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             });
             if (configured != cudaSuccess)
             {
                 return configured;
             }
-            tc_group_kernel<DC, R, IN, OUT, NS, Contig><<<grid, tc_workers<Contig> + 32, smem, stream>>>(p);
+            tc_group_kernel<DC, R, IN, OUT, NS, Contig, Lay><<<grid, tc_workers<Contig> + 32, smem, stream>>>(p);
             return cudaGetLastError();
         }
 
@@ -72,27 +72,43 @@ namespace hmpc_gb300
             out.splits = NS;
         }
 
-        // the instantiated shapes: every (R, input, output, splits, contiguous) a plan uses
+        // the instantiated shapes: every (R, input, output, splits, contiguous,
+        // record layout) a plan uses
         template<typename F>
-        bool dispatch(int r, int in_kind, int out_kind, int splits, bool contig, F& f)
+        bool dispatch(int r, int in_kind, int out_kind, int splits, bool contig, int lay, F& f)
         {
-            if (out_kind == tc_out_digits && r == 8)
+            if (out_kind == tc_out_digits && r == 8 && !contig && splits == 1)
             {
-                if (in_kind == tc_in_limbs && splits == 1 && !contig) return f.template run<8, tc_in_limbs, tc_out_digits, 1, false>();
-                if (in_kind == tc_in_limbs && splits == 2 && contig) return f.template run<8, tc_in_limbs, tc_out_digits, 2, true>();
-                if (in_kind == tc_in_limbs && splits == 1 && contig) return f.template run<8, tc_in_limbs, tc_out_digits, 1, true>();
-                if (in_kind == tc_in_cbd && splits == 1 && !contig) return f.template run<8, tc_in_cbd, tc_out_digits, 1, false>();
-                if (in_kind == tc_in_digits && splits == 1 && !contig) return f.template run<8, tc_in_digits, tc_out_digits, 1, false>();
+                if (in_kind == tc_in_limbs) return lay ? f.template run<8, tc_in_limbs, tc_out_digits, 1, false, 2>()
+                                                       : f.template run<8, tc_in_limbs, tc_out_digits, 1, false, 0>();
+                if (in_kind == tc_in_cbd) return lay ? f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 2>()
+                                                     : f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 0>();
+                if (in_kind == tc_in_digits) return lay ? f.template run<8, tc_in_digits, tc_out_digits, 1, false, 2>()
+                                                        : f.template run<8, tc_in_digits, tc_out_digits, 1, false, 0>();
+            }
+            if (out_kind == tc_out_digits && r == 8 && contig && in_kind == tc_in_limbs && lay == 0)
+            {
+                if (splits == 2) return f.template run<8, tc_in_limbs, tc_out_digits, 2, true, 0>();
+                if (splits == 1) return f.template run<8, tc_in_limbs, tc_out_digits, 1, true, 0>();
             }
             if (out_kind == tc_out_limbs && in_kind == tc_in_digits)
             {
-                if (r == 8 && splits == 1) return contig ? f.template run<8, tc_in_digits, tc_out_limbs, 1, true>()
-                                                         : f.template run<8, tc_in_digits, tc_out_limbs, 1, false>();
-                if (r == 8 && splits == 2 && contig) return f.template run<8, tc_in_digits, tc_out_limbs, 2, true>();
-                if (r == 4 && splits == 1) return contig ? f.template run<4, tc_in_digits, tc_out_limbs, 1, true>()
-                                                         : f.template run<4, tc_in_digits, tc_out_limbs, 1, false>();
-                if (r == 2 && splits == 1) return contig ? f.template run<2, tc_in_digits, tc_out_limbs, 1, true>()
-                                                         : f.template run<2, tc_in_digits, tc_out_limbs, 1, false>();
+                if (lay == 1 && contig && splits == 1)
+                {
+                    if (r == 8) return f.template run<8, tc_in_digits, tc_out_limbs, 1, true, 1>();
+                    if (r == 4) return f.template run<4, tc_in_digits, tc_out_limbs, 1, true, 1>();
+                    if (r == 2) return f.template run<2, tc_in_digits, tc_out_limbs, 1, true, 1>();
+                }
+                if (lay == 0)
+                {
+                    if (r == 8 && splits == 2 && contig) return f.template run<8, tc_in_digits, tc_out_limbs, 2, true, 0>();
+                    if (r == 8 && splits == 1) return contig ? f.template run<8, tc_in_digits, tc_out_limbs, 1, true, 0>()
+                                                             : f.template run<8, tc_in_digits, tc_out_limbs, 1, false, 0>();
+                    if (r == 4 && splits == 1) return contig ? f.template run<4, tc_in_digits, tc_out_limbs, 1, true, 0>()
+                                                             : f.template run<4, tc_in_digits, tc_out_limbs, 1, false, 0>();
+                    if (r == 2 && splits == 1) return contig ? f.template run<2, tc_in_digits, tc_out_limbs, 1, true, 0>()
+                                                             : f.template run<2, tc_in_digits, tc_out_limbs, 1, false, 0>();
+                }
             }
             return false;
         }
@@ -104,10 +120,10 @@ namespace hmpc_gb300
             cudaStream_t stream;
             cudaError_t e;
 
-            template<int R, int IN, int OUT, int NS, bool Contig>
+            template<int R, int IN, int OUT, int NS, bool Contig, int Lay>
             bool run()
             {
-                e = launch<R, IN, OUT, NS, Contig>(p, grid, stream);
+                e = launch<R, IN, OUT, NS, Contig, Lay>(p, grid, stream);
                 return true;
             }
         };
@@ -116,7 +132,7 @@ namespace hmpc_gb300
         {
             TcShapeInfo& out;
 
-            template<int R, int IN, int OUT, int NS, bool Contig>
+            template<int R, int IN, int OUT, int NS, bool Contig, int Lay>
             bool run()
             {
                 fill<R, IN, NS>(out);
@@ -124,19 +140,20 @@ namespace hmpc_gb300
             }
         };
 
-        cudaError_t group(const TcGroupParams& p, int r, int in_kind, int out_kind, int splits, unsigned grid,
-                          cudaStream_t stream)
+        cudaError_t group(const TcGroupParams& p, int r, int in_kind, int out_kind, int splits, int layout,
+                          unsigned grid, cudaStream_t stream)
         {
             Launcher f{p, grid, stream, cudaErrorInvalidValue};
-            dispatch(r, in_kind, out_kind, splits, p.lo == 0, f);
+            dispatch(r, in_kind, out_kind, splits, p.lo == 0, layout, f);
             return f.e;
         }
 
         bool shape(int r, int in_kind, int out_kind, int splits, TcShapeInfo& out)
         {
             Filler f{out};
-            return dispatch(r, in_kind, out_kind, splits, splits == 2, f) ||
-                   dispatch(r, in_kind, out_kind, splits, false, f) || dispatch(r, in_kind, out_kind, splits, true, f);
+            return dispatch(r, in_kind, out_kind, splits, splits == 2, 0, f) ||
+                   dispatch(r, in_kind, out_kind, splits, false, 0, f) ||
+                   dispatch(r, in_kind, out_kind, splits, true, 0, f);
         }
 
         unsigned blocks_for(uint64_t threads)

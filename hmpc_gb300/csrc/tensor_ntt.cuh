@@ -42,6 +42,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include <cuda_fp16.h>
 
@@ -89,6 +90,7 @@ namespace hmpc_gb300
         uint32_t nw;
         uint32_t q[8];             // final reduction
         float inv_q_top;           // 2^(32(L-1)) / q
+        uint32_t block_shift;      // blocked digit planes: log2 of the elements per block
     };
 
     // Sizes of one group kernel.  NS splits a block's R output elements over
@@ -182,7 +184,9 @@ namespace hmpc_gb300
 
     // loader of digit / limb tiles: thread (row, part) owns words part, part +
     // tc_parts, ... of the row's R elements
-    template<int DC, int R, int IN, int NS, int Parts>
+    // InBlk: the input digit planes are blocked per R adjacent elements (word w
+    // of element e at (e - e mod R) * W + w * R + e mod R): a row is one run
+    template<int DC, int R, int IN, int NS, int Parts, bool InBlk = false>
     struct TcLoader
     {
         using S = TcShape<DC, R, IN, NS>;
@@ -190,9 +194,9 @@ namespace hmpc_gb300
         static constexpr int wh = S::w_in > 0 ? (S::w_in + tc_parts - 1) / tc_parts : 1;
         uint32_t v[wh][R];
 
-        __device__ __forceinline__ void load(const TcGroupParams& p, uint64_t h, uint32_t mt, uint32_t row,
-                                             uint32_t part)
+        __device__ __forceinline__ void load(const TcGroupParams& p, uint64_t h, uint32_t mt, uint32_t tid)
         {
+            const uint32_t row = tid % tc_rows, part = tid / tc_rows;
             const TcRow r = tc_row<S::g>(p, h, mt, row);
             const uint32_t* rp = p.in + r.base;
             const bool contiguous = p.lo == 0;  // the row's R elements are adjacent: vector loads
@@ -201,7 +205,7 @@ namespace hmpc_gb300
             {
                 const uint32_t w = part + tc_parts * wi;
                 const bool live = r.ok && w < static_cast<uint32_t>(S::w_in);
-                const uint32_t* wp = rp + w * p.elements;
+                const uint32_t* wp = InBlk ? p.in + r.base * S::w_in + w * R : rp + w * p.elements;
                 if (live && contiguous)
                 {
                     if constexpr (R == 8)
@@ -233,8 +237,9 @@ namespace hmpc_gb300
             }
         }
 
-        __device__ __forceinline__ void store(uint8_t* sa, uint32_t row, uint32_t part) const
+        __device__ __forceinline__ void store(uint8_t* sa, uint32_t tid) const
         {
+            const uint32_t row = tid % tc_rows, part = tid / tc_rows;
             constexpr int bias = IN == tc_in_digits ? 128 : 0;
 #pragma unroll
             for (int wi = 0; wi < wh; ++wi)
@@ -288,16 +293,21 @@ namespace hmpc_gb300
         }
     };
 
-    // first forward group fed by centred binomial samples: r = 8, stage-0 pairs
-    // (m, m + 4) of a row come from one generator with counter = poly * N +
-    // index of the first element, first draw for m, second for m + 4
-    // (number_theoretic_transform.hpp:316-329, comp/queue.hpp:191-212); thread
-    // (row, part) draws the pair m = part
     __device__ __forceinline__ void st_shared_u16(uint8_t* p, uint16_t a)
     {
         asm volatile("st.shared.u16 [%0], %1;" ::"r"(tc::smem_u32(p)), "h"(a) : "memory");
     }
 
+    __device__ __forceinline__ void st_shared_v2(uint8_t* p, uint32_t a, uint32_t b)
+    {
+        asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(tc::smem_u32(p)), "r"(a), "r"(b) : "memory");
+    }
+
+    // first forward group fed by centred binomial samples: r = 8, stage-0 pairs
+    // (m, m + 4) of a row come from one generator with counter = poly * N +
+    // index of the first element, first draw for m, second for m + 4
+    // (number_theoretic_transform.hpp:316-329, comp/queue.hpp:191-212); thread
+    // (row, part) draws the pair m = part
     __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t row,
                                                  uint32_t part)
     {
@@ -447,7 +457,7 @@ namespace hmpc_gb300
     // carry the accumulator of one tile out of TMEM: each thread owns one row
     // and `per` consecutive output elements of the block's split; Contig: the
     // row's elements are adjacent (no column bits), stored as vectors
-    template<int DC, int R, int OUT, int NS, bool Contig>
+    template<int DC, int R, int OUT, int NS, bool Contig, bool OutRec>
     __device__ __forceinline__ void tc_epilogue(const TcGroupParams& p, uint32_t tmem, const TcCursor& cur,
                                                 uint32_t warp, uint32_t lane)
     {
@@ -525,10 +535,26 @@ namespace hmpc_gb300
             else if (r.ok)
             {
                 const uint64_t e = static_cast<uint64_t>(k0 + kk) << p.lo;
-#pragma unroll
-                for (int w = 0; w < words_out; ++w)
+                if constexpr (OutRec)
                 {
-                    op[w * p.elements + e] = words[w];
+                    // digit planes blocked per 2^block_shift elements, for a next
+                    // group whose rows are that many adjacent elements
+                    const uint64_t ea = r.base + e;
+                    const uint64_t m = ea & ((1ull << p.block_shift) - 1ull);
+                    uint32_t* blk = p.out + (ea - m) * W + m;
+#pragma unroll
+                    for (int w = 0; w < words_out; ++w)
+                    {
+                        blk[static_cast<uint64_t>(w) << p.block_shift] = words[w];
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int w = 0; w < words_out; ++w)
+                    {
+                        op[w * p.elements + e] = words[w];
+                    }
                 }
             }
         }
@@ -558,7 +584,9 @@ namespace hmpc_gb300
     // accumulators (full: MMA commit; empty: 512 arrivals) and the constant
     // buffers (transaction count).  Every wait is bounded; a timeout sets the
     // error word and both sides leave their loops.
-    template<int DC, int R, int IN, int OUT, int NS, bool Contig>
+    // Lay bit 0: the input digit planes are blocked per R adjacent elements;
+    // bit 1: the output planes are blocked for the next group
+    template<int DC, int R, int IN, int OUT, int NS, bool Contig, int Lay>
     __global__ void __launch_bounds__(tc_workers<Contig> + 32, 1) tc_group_kernel(const TcGroupParams p)
     {
         using S = TcShape<DC, R, IN, NS>;
@@ -753,13 +781,15 @@ namespace hmpc_gb300
         {
             // ------------------------------------------------ workers
             const uint32_t row = tid & (tc_rows - 1), part = tid / tc_rows;
-            TcLoader<DC, R, IN, NS, tc_threads / tc_rows> loader;
+            constexpr bool in_blk = (Lay & 1) != 0;
+            static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
+            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk> loader;
             TcCursor cur = first;
             if constexpr (IN != tc_in_cbd)
             {
                 if (count)
                 {
-                    loader.load(p, cur.hb / NS, cur.mt, row, part);
+                    loader.load(p, cur.hb / NS, cur.mt, tid);
                 }
             }
             TcCursor prev = cur;
@@ -787,7 +817,7 @@ namespace hmpc_gb300
                     }
                     else
                     {
-                        loader.store(sa, row, part);
+                        loader.store(sa, tid);
                     }
                     tc::fence_proxy_async();
                     mbar_arrive(bar_a_full);
@@ -796,7 +826,7 @@ namespace hmpc_gb300
                         if (i + 1 < count)
                         {
                             const TcCursor n1 = cur.next(tpb);
-                            loader.load(p, n1.hb / NS, n1.mt, row, part);
+                            loader.load(p, n1.hb / NS, n1.mt, tid);
                         }
                     }
                 }
@@ -816,7 +846,7 @@ namespace hmpc_gb300
                         break;
                     }
                     tc::fence_after_sync();
-                    tc_epilogue<DC, R, OUT, NS, Contig>(p, tmem + acc * S::cols, prev, warp, lane);
+                    tc_epilogue<DC, R, OUT, NS, Contig, (Lay & 2) != 0>(p, tmem + acc * S::cols, prev, warp, lane);
                     tc::fence_before_sync();
                     mbar_arrive(&bar_acc_empty[acc]);
                 }
