@@ -5,9 +5,12 @@
 // representation as hmpc's mod<Q> (hmpc/ints/mod.hpp:73-193), so any exact
 // implementation of the operations below reproduces the reference bit for bit.
 //
-// Carry propagation uses PTX carry chains (add.cc / addc / mad.lo.cc /
-// madc.hi.cc).  Each chain is a run of consecutive volatile asm statements; no
-// other instruction in between touches the condition code.
+// Additions, subtractions and the wide reduction use PTX carry chains
+// (add.cc / addc / sub.cc / subc / mad.lo.cc / madc.hi.cc); each chain is a run
+// of consecutive volatile asm statements with no other instruction between
+// them touching the condition code.  The Montgomery product is CIOS written as
+// 64-bit multiply-adds, which a throughput probe measured faster than the
+// carry-chain form.
 #pragma once
 
 #include <cstdint>
