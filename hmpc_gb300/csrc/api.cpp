@@ -78,7 +78,7 @@ namespace hmpc_gb300::detail
 
     int run_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                       uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out, const uint32_t* poly_rng,
-                      uint32_t rng_slot)
+                      uint32_t rng_slot, bool cuda_cores_only)
     {
         if (int rc = enter(ctx))
         {
@@ -155,7 +155,7 @@ namespace hmpc_gb300::detail
         if (choice.radix_bits == 0)
         {
             // tensor-core engine; calls it does not cover run the default CUDA-core tiles
-            if (tc_applicable(mod, log_n, kind, poly_rng))
+            if (!cuda_cores_only && tc_applicable(mod, log_n, kind, poly_rng))
             {
                 return run_tc_transform(ctx, mod, n, batch, inverse, kind, vx2, src, out, choice.local_bits);
             }
@@ -1079,6 +1079,49 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
     uint32_t* v = ws + poly_words;
     uint32_t* msg = ws + 2 * poly_words;
     uint32_t* coeff = ws + 3 * poly_words;
+    const int tc_splits = tc_plan_splits(q, n, batch);
+    if (tc_splits && n >= 16 && tc_supported(q) && p->c.limbs <= 2)
+    {
+        // Tensor-core plan for q: the NTT is linear, so p*NTT(v) + NTT(lift(m))
+        // is one transform of the small integers p*v + lift(m) drawn and lifted
+        // in its first group, and p*NTT(w) one of p*w: three transforms and two
+        // one-product combines, the same ciphertext bit for bit (every result
+        // is the reduced representative).  RNG order as the reference's plan:
+        // u, v, w (expr/cache.hpp:226-271).
+        int rc = run_transform(ctx, q, n, batch, false, producer_cbd, 1, 0, nullptr, u);
+        const uint32_t* coefficients = plaintext;
+        if (!rc && plaintext_ntt)
+        {
+            rc = run_transform(ctx, p, n, batch, true, producer_tensor, 0, 0, plaintext, coeff);
+            coefficients = coeff;
+        }
+        TcSmallInput with_msg{coefficients, p};
+        if (!rc)
+        {
+            rc = run_tc_transform(ctx, q, n, batch, false, producer_cbd, 20, nullptr, v, tc_splits, &with_msg);
+        }
+        if (!rc)
+        {
+            cudaError_t e = q->kt->lhe_combine_sum(c0, key_a, n, u, v, elements, q->h, ctx->stream);
+            if (e != cudaSuccess)
+            {
+                return cuda_fail(e, "launching combine");
+            }
+            ++ctx->launches;
+            TcSmallInput no_msg{nullptr, p};
+            rc = run_tc_transform(ctx, q, n, batch, false, producer_cbd, 20, nullptr, v, tc_splits, &no_msg);
+        }
+        if (!rc)
+        {
+            cudaError_t e = q->kt->lhe_combine_sum(c1, key_b, n, u, v, elements, q->h, ctx->stream);
+            if (e != cudaSuccess)
+            {
+                return cuda_fail(e, "launching combine");
+            }
+            ++ctx->launches;
+        }
+        return rc;
+    }
     // the execution order of the reference's plan: NTT(u), NTT(v),
     // [INTT_p(x)], NTT_q(msg), c0, NTT(w), c1 (expr/cache.hpp:226-271)
     int rc = run_transform(ctx, q, n, batch, false, producer_cbd, 1, 0, nullptr, u);

@@ -49,6 +49,16 @@ namespace hmpc_gb300::detail
         size_t bytes = 0;
         uint8_t* first_cbd = nullptr;  // first group fed by centred binomial samples
         TcShapeInfo cbd_shape;
+        uint8_t* first_small = nullptr;  // first group fed by p * sample + lift(plaintext)
+        TcShapeInfo small_shape;
+    };
+
+    // first group of a forward transform fed by x = p * CBD(V) + lift(m):
+    // plaintext residues m mod p (nullptr: none) and the plaintext modulus
+    struct TcSmallInput
+    {
+        const uint32_t* msg = nullptr;
+        const hmpc_modulus* p = nullptr;
     };
 }
 
@@ -152,6 +162,7 @@ struct hmpc_modulus
         {
             cudaFree(kv.second.images);
             cudaFree(kv.second.first_cbd);
+            cudaFree(kv.second.first_small);
         }
     }
 
@@ -206,9 +217,10 @@ namespace hmpc_gb300::detail
 {
     int check_degree(uint64_t n);
     int enter(hmpc_context* ctx);
+    // cuda_cores_only: ignore a tensor-core plan (callers that must not allocate)
     int run_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                       uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out,
-                      const uint32_t* poly_rng = nullptr, uint32_t rng_slot = 0);
+                      const uint32_t* poly_rng = nullptr, uint32_t rng_slot = 0, bool cuda_cores_only = false);
     int run_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                   uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
     CastParams make_cast(const hmpc_modulus* dst, const hmpc_modulus* src);
@@ -220,6 +232,9 @@ namespace hmpc_gb300::detail
     bool tc_applicable(const hmpc_modulus* mod, int log_n, int kind, const uint32_t* poly_rng);
     // splits: output split of the group whose rows are contiguous (1 or 2)
     int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
-                         uint32_t vx2, const uint32_t* src, uint32_t* out, int splits);
+                         uint32_t vx2, const uint32_t* src, uint32_t* out, int splits,
+                         const TcSmallInput* small = nullptr);
+    // the tensor-core plan of (n, batch, forward) if one is set for the modulus: splits, else 0
+    int tc_plan_splits(hmpc_modulus* mod, uint64_t n, uint64_t batch);
     int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out);
 }

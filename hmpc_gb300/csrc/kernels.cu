@@ -350,9 +350,21 @@ namespace hmpc_gb300
             return e == cudaSuccess ? blocks : 0;
         }
 
+        cudaError_t lhe_combine_sum(uint32_t* out, const uint32_t* kp, uint64_t n, const uint32_t* u,
+                                    const uint32_t* x, uint64_t elements, const HostModulus& h, cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            lhe_combine_sum_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, kp, n, u, x, elements,
+                                                                                  device_modulus(h));
+            return cudaGetLastError();
+        }
+
         const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd, to_montgomery,
                                    from_montgomery, cast, plain_stage, ct_mul, dec_combine, ntt_batched,
-                                   ntt_batched_blocks_per_sm, R};
+                                   ntt_batched_blocks_per_sm, R, lhe_combine_sum};
     }
 
     const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()

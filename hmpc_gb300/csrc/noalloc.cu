@@ -110,15 +110,15 @@ extern "C" int hmpc_lhe_enc_noalloc(hmpc_context* ctx, hmpc_modulus* q, hmpc_mod
     uint32_t* coeff = scratch + 3 * poly_words;
     // the reference's execution order: NTT(u), NTT(v), [INTT_p(x)],
     // NTT_q(msg), c0, NTT(w), c1 (expr/cache.hpp:226-271)
-    int rc = run_transform(ctx, q, n, batch, false, producer_cbd, 1, 0, nullptr, u);
+    int rc = run_transform(ctx, q, n, batch, false, producer_cbd, 1, 0, nullptr, u, nullptr, 0, true);
     if (!rc)
     {
-        rc = run_transform(ctx, q, n, batch, false, producer_cbd, 20, 0, nullptr, v);
+        rc = run_transform(ctx, q, n, batch, false, producer_cbd, 20, 0, nullptr, v, nullptr, 0, true);
     }
     const uint32_t* coefficients = plaintext;
     if (!rc && plaintext_ntt)
     {
-        rc = run_transform(ctx, p, n, batch, true, producer_tensor, 0, 0, plaintext, coeff);
+        rc = run_transform(ctx, p, n, batch, true, producer_tensor, 0, 0, plaintext, coeff, nullptr, 0, true);
         coefficients = coeff;
     }
     if (rc)
@@ -131,7 +131,7 @@ extern "C" int hmpc_lhe_enc_noalloc(hmpc_context* ctx, hmpc_modulus* q, hmpc_mod
         return cuda_fail(e, "launching cast");
     }
     ++ctx->launches;
-    if ((rc = run_transform(ctx, q, n, batch, false, producer_tensor, 0, 0, msg, msg)))
+    if ((rc = run_transform(ctx, q, n, batch, false, producer_tensor, 0, 0, msg, msg, nullptr, 0, true)))
     {
         return rc;
     }
@@ -142,7 +142,7 @@ extern "C" int hmpc_lhe_enc_noalloc(hmpc_context* ctx, hmpc_modulus* q, hmpc_mod
         return cuda_fail(e, "launching combine");
     }
     ++ctx->launches;
-    if ((rc = run_transform(ctx, q, n, batch, false, producer_cbd, 20, 0, nullptr, v)))  // w reuses v
+    if ((rc = run_transform(ctx, q, n, batch, false, producer_cbd, 20, 0, nullptr, v, nullptr, 0, true)))  // w reuses v
     {
         return rc;
     }

@@ -93,7 +93,7 @@ namespace
     }
 
     int prepare_tc(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, int splits, bool need_cbd,
-                   TcTables** out)
+                   bool need_small, TcTables** out)
     {
         Tables* t = nullptr;
         if (int rc = mod->prepare(n, &t))
@@ -107,7 +107,7 @@ namespace
         auto key = std::make_tuple(log_n, inverse ? 1 : 0, splits);
         auto it = mod->tc_tables.find(key);
         const bool fresh = it == mod->tc_tables.end();
-        if (!fresh && (!need_cbd || it->second.first_cbd))
+        if (!fresh && (!need_cbd || it->second.first_cbd) && (!need_small || it->second.first_small))
         {
             *out = &it->second;
             return HMPC_OK;
@@ -205,6 +205,25 @@ namespace
                 return rc;
             }
         }
+        if (need_small && !tt.first_small)
+        {
+            // first forward group fed by x = p * sample + lift(m): constants G * R * 256^a, 9 digit slots
+            k->shape(8, tc_in_small, tc_out_digits, 1, tt.small_shape);
+            TcGroupPlan gp = tt.groups.front();
+            gp.shape = tt.small_shape;
+            if (cudaMalloc(&tt.first_small, tt.small_shape.b_bytes) != cudaSuccess)
+            {
+                cleanup();
+                return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core constants");
+            }
+            cudaMemsetAsync(tt.first_small, 0, tt.small_shape.b_bytes, ctx->stream);
+            if (int rc = build_group(ctx, mod, t, log_n, inverse, gp, true, tc_small_digits, tt.first_small, d_gx,
+                                     d_pow))
+            {
+                cleanup();
+                return rc;
+            }
+        }
         cleanup();
         if (cudaGetLastError() != cudaSuccess)
         {
@@ -241,9 +260,13 @@ namespace hmpc_gb300::detail
     }
 
     int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
-                         uint32_t vx2, const uint32_t* src, uint32_t* out, int splits)
+                         uint32_t vx2, const uint32_t* src, uint32_t* out, int splits, const TcSmallInput* small)
     {
         const bool cbd = kind == producer_cbd;
+        if (small && (!cbd || inverse || !small->p || small->p->c.limbs > 2))
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "the small-integer first group needs a forward CBD transform and p < 2^64");
+        }
         if (cbd && (vx2 < 1 || vx2 > 64))
         {
             return fail(HMPC_ERROR_UNSUPPORTED, "centred binomial needs 1 <= 2V <= 64");
@@ -253,7 +276,7 @@ namespace hmpc_gb300::detail
         {
             splits = 1;
         }
-        if (int rc = prepare_tc(ctx, mod, n, inverse, splits, cbd, &tt))
+        if (int rc = prepare_tc(ctx, mod, n, inverse, splits, cbd && !small, small != nullptr, &tt))
         {
             return rc;
         }
@@ -292,7 +315,7 @@ namespace hmpc_gb300::detail
             TcGroupParams p{};
             p.in = j == 0 ? src : digits + (((j - 1) & 1u) ? static_cast<uint64_t>(w) * elements : 0);
             p.out = j + 1 == stages ? out : digits + ((j & 1u) ? static_cast<uint64_t>(w) * elements : 0);
-            p.images = (j == 0 && cbd) ? tt->first_cbd : tt->images + gp.offset;
+            p.images = (j == 0 && cbd) ? (small ? tt->first_small : tt->first_cbd) : tt->images + gp.offset;
             p.error = ctx->tc_error;
             p.elements = elements;
             p.rows = batch << gp.lo;
@@ -310,8 +333,21 @@ namespace hmpc_gb300::detail
             }
             p.inv_q_top = inv_q_top;
             p.block_shift = tt->groups.back().g;  // the last group's elements per row
+            if (small)
+            {
+                const hmpc_modulus* pm = small->p;
+                p.msg = small->msg;
+                p.msg_limbs = static_cast<uint32_t>(pm->c.limbs);
+                p.pninv = pm->c.ninv;
+                for (int i = 0; i < pm->c.limbs; ++i)
+                {
+                    p.pq[i] = pm->c.q[static_cast<size_t>(i)];
+                    p.phalf[i] = pm->c.half[static_cast<size_t>(i)];
+                }
+            }
             const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
-            const int in_kind = j == 0 ? (cbd ? static_cast<int>(tc_in_cbd) : static_cast<int>(tc_in_limbs))
+            const int in_kind = j == 0 ? (cbd ? static_cast<int>(small ? tc_in_small : tc_in_cbd)
+                                              : static_cast<int>(tc_in_limbs))
                                        : static_cast<int>(tc_in_digits);
             const int splits = (j == 0 && cbd) ? 1 : static_cast<int>(gp.shape.splits);
             cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, gp.layout, grid, ctx->stream);
@@ -360,6 +396,17 @@ namespace hmpc_gb300::detail
             out->flops += tiles * 2.0 * tc_rows * shape.n_mma * shape.k_pad;
         }
         return HMPC_OK;
+    }
+
+    int tc_plan_splits(hmpc_modulus* mod, uint64_t n, uint64_t batch)
+    {
+        std::lock_guard<std::mutex> lock(mod->tables_mutex);
+        auto it = mod->tile_choices.find(std::make_tuple(__builtin_ctzll(n), 0, batch));
+        if (it == mod->tile_choices.end() || it->second.radix_bits != 0)
+        {
+            return 0;
+        }
+        return it->second.local_bits == 2 ? 2 : 1;
     }
 }
 

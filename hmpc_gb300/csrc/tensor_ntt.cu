@@ -83,6 +83,8 @@ namespace hmpc_gb300
                                                        : f.template run<8, tc_in_limbs, tc_out_digits, 1, false, 0>();
                 if (in_kind == tc_in_cbd) return lay ? f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 2>()
                                                      : f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 0>();
+                if (in_kind == tc_in_small) return lay ? f.template run<8, tc_in_small, tc_out_digits, 1, false, 2>()
+                                                       : f.template run<8, tc_in_small, tc_out_digits, 1, false, 0>();
                 if (in_kind == tc_in_digits) return lay ? f.template run<8, tc_in_digits, tc_out_digits, 1, false, 2>()
                                                         : f.template run<8, tc_in_digits, tc_out_digits, 1, false, 0>();
             }

@@ -57,6 +57,7 @@ namespace hmpc_gb300
         tc_in_digits = 0,  // digit words of the previous group
         tc_in_limbs = 1,   // limb-planar residues (unsigned bytes)
         tc_in_cbd = 2,     // centred binomial samples drawn in the loader
+        tc_in_small = 3,   // x = p * CBD sample + centred lift of a residue mod p, computed in the loader
     };
 
     enum TcOutput : int
@@ -91,7 +92,17 @@ namespace hmpc_gb300
         uint32_t q[8];             // final reduction
         float inv_q_top;           // 2^(32(L-1)) / q
         uint32_t block_shift;      // blocked digit planes: log2 of the elements per block
+        // small-integer loader: plaintext residues mod p (msg_limbs planes of
+        // `elements` words, Montgomery form; nullptr: none) and p's constants
+        const uint32_t* msg;
+        uint32_t msg_limbs;
+        uint32_t pq[2];
+        uint32_t pninv;
+        uint32_t phalf[2];
     };
+
+    // balanced base-256 digits of the small-integer input (|x| < 2^70 for p < 2^64, 2V <= 64)
+    constexpr int tc_small_digits = 9;
 
     // Sizes of one group kernel.  NS splits a block's R output elements over
     // NS constant images (N = R / NS * DC columns each); NBUF constant buffers
@@ -101,10 +112,12 @@ namespace hmpc_gb300
     struct TcShape
     {
         static constexpr int g = R == 8 ? 3 : (R == 4 ? 2 : 1);
-        static constexpr int d_in = IN == tc_in_digits ? DC + 2 : (IN == tc_in_limbs ? DC : 1);
-        static constexpr int w_in = IN == tc_in_cbd ? 0 : (d_in + 3) / 4;
+        static constexpr int d_in = IN == tc_in_digits ? DC + 2
+                                    : (IN == tc_in_limbs ? DC : (IN == tc_in_small ? tc_small_digits : 1));
+        static constexpr bool generated = IN == tc_in_cbd || IN == tc_in_small;  // no input planes
+        static constexpr int w_in = generated ? 0 : (d_in + 3) / 4;
         // digit slots per element on the K axis (K index = a * R + m)
-        static constexpr int d_eff = IN == tc_in_cbd ? 1 : (R == 8 ? d_in : (R == 4 ? (d_in + 1) / 2 * 2 : w_in * 4));
+        static constexpr int d_eff = generated ? d_in : (R == 8 ? d_in : (R == 4 ? (d_in + 1) / 2 * 2 : w_in * 4));
         static constexpr int k_real = R * d_eff;
         static constexpr int k_pad = (k_real + 15) / 16 * 16;
         static constexpr int outputs = R / NS;  // output elements per N-split
@@ -344,6 +357,98 @@ namespace hmpc_gb300
         const __half hu = __int2half_rn(e_u), hv = __int2half_rn(e_v);
         st_shared_u16(seg + 2 * part, *reinterpret_cast<const uint16_t*>(&hu));
         st_shared_u16(seg + 8 + 2 * part, *reinterpret_cast<const uint16_t*>(&hv));
+    }
+
+    // canonical value of a residue mod p (one or two limbs, Montgomery form),
+    // lifted to the centred integer in (-p/2, p/2] (hmpc/ints/mod.hpp:259-307:
+    // the canonical value v becomes v - p when v > floor(p/2))
+    __device__ __forceinline__ long long tc_centred_lift(const TcGroupParams& p, uint64_t e)
+    {
+        const int lp = static_cast<int>(p.msg_limbs);
+        uint32_t t[5] = {p.msg[e], lp > 1 ? p.msg[p.elements + e] : 0u, 0u, 0u, 0u};
+        // word-by-word Montgomery reduction by 2^(32 lp) (core/num/modulo.hpp:30-66)
+        for (int i = 0; i < lp; ++i)
+        {
+            const uint32_t mq = t[i] * p.pninv;
+            uint64_t carry = 0;
+            for (int j = 0; j < lp; ++j)
+            {
+                const uint64_t s = static_cast<uint64_t>(mq) * p.pq[j] + t[i + j] + carry;
+                t[i + j] = static_cast<uint32_t>(s);
+                carry = s >> 32;
+            }
+            for (int k = i + lp; k < 5; ++k)
+            {
+                const uint64_t s = static_cast<uint64_t>(t[k]) + carry;
+                t[k] = static_cast<uint32_t>(s);
+                carry = s >> 32;
+            }
+        }
+        const uint64_t q = p.pq[0] | (lp > 1 ? static_cast<uint64_t>(p.pq[1]) << 32 : 0ull);
+        const uint64_t half = p.phalf[0] | (lp > 1 ? static_cast<uint64_t>(p.phalf[1]) << 32 : 0ull);
+        uint64_t v = t[lp] | (lp > 1 ? static_cast<uint64_t>(t[lp + 1]) << 32 : 0ull);
+        if (t[2 * lp] || v >= q)
+        {
+            v -= q;
+        }
+        return v > half ? static_cast<long long>(v) - static_cast<long long>(q) : static_cast<long long>(v);
+    }
+
+    // first forward group fed by x = p * e + lift(m): e drawn as the CBD
+    // loader draws it (one generator per stage-0 pair, thread (row, part) draws
+    // the pair m = part, m + 4), m the plaintext residue of the same element;
+    // x is written as 9 balanced base-256 digits (K index = a * 8 + m)
+    __device__ __forceinline__ void tc_store_small(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t row,
+                                                   uint32_t part)
+    {
+        const TcRow r = tc_row<3>(p, 0, mt, row);
+        __int128 x[2] = {0, 0};
+        if (r.ok)
+        {
+            const int count = 2 * static_cast<int>(p.vx2);
+            const int nw = static_cast<int>(p.nw);
+            const uint64_t idx = r.base + (static_cast<uint64_t>(part) << p.lo);
+            uint32_t w[8];
+            chacha_stream<8>(p.rng, static_cast<uint32_t>(idx), w);
+            int a = 0, b = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+            {
+                const int iv = i - nw;
+                uint32_t mu = 0u, mv = 0u;
+                if (i < nw)
+                {
+                    mu = (i == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
+                }
+                else if (iv < nw)
+                {
+                    mv = (iv == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
+                }
+                a += __popc(w[i] & mu);
+                b += __popc(w[i] & mv);
+            }
+            const uint64_t pval = p.pq[0] | (p.msg_limbs > 1 ? static_cast<uint64_t>(p.pq[1]) << 32 : 0ull);
+            x[0] = static_cast<__int128>(pval) * (a - static_cast<int>(p.vx2));
+            x[1] = static_cast<__int128>(pval) * (b - static_cast<int>(p.vx2));
+            if (p.msg)
+            {
+                x[0] += tc_centred_lift(p, idx);
+                x[1] += tc_centred_lift(p, idx + (4ull << p.lo));
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < tc_small_digits; ++d)
+        {
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+            {
+                const int digit = static_cast<int>(static_cast<uint32_t>(x[j] + 128) & 255u) - 128;
+                x[j] = (x[j] - digit) >> 8;
+                const __half h = __int2half_rn(digit);
+                st_shared_u16(sa + tc::operand_offset(row, d * 8 + part + 4 * j, tc_rows),
+                              *reinterpret_cast<const uint16_t*>(&h));
+            }
+        }
     }
 
     __device__ __forceinline__ uint32_t pack_bytes(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3)
@@ -591,7 +696,8 @@ namespace hmpc_gb300
     {
         using S = TcShape<DC, R, IN, NS>;
         constexpr int tc_threads = tc_workers<Contig>;
-        static_assert(IN != tc_in_cbd || tc_threads / tc_rows == 4, "the CBD loader draws one pair per thread");
+        static_assert(!TcShape<DC, R, IN, NS>::generated || tc_threads / tc_rows == 4,
+                      "the sampling loaders draw one pair per thread");
         constexpr int NBUF = S::nbuf;
         extern __shared__ __align__(1024) uint8_t tc_smem[];
         uint8_t* sb = tc_smem;                           // NBUF constant buffers
@@ -785,7 +891,7 @@ namespace hmpc_gb300
             static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
             TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk> loader;
             TcCursor cur = first;
-            if constexpr (IN != tc_in_cbd)
+            if constexpr (!S::generated)
             {
                 if (count)
                 {
@@ -815,13 +921,17 @@ namespace hmpc_gb300
                     {
                         tc_store_cbd(p, sa, cur.mt, row, part);
                     }
+                    else if constexpr (IN == tc_in_small)
+                    {
+                        tc_store_small(p, sa, cur.mt, row, part);
+                    }
                     else
                     {
                         loader.store(sa, tid);
                     }
                     tc::fence_proxy_async();
                     mbar_arrive(bar_a_full);
-                    if constexpr (IN != tc_in_cbd)
+                    if constexpr (!S::generated)
                     {
                         if (i + 1 < count)
                         {
