@@ -1084,36 +1084,38 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
     {
         // Tensor-core plan for q: the NTT is linear, so p*NTT(v) + NTT(lift(m))
         // is one transform of the small integers p*v + lift(m) drawn and lifted
-        // in its first group, and p*NTT(w) one of p*w: three transforms and two
-        // one-product combines, the same ciphertext bit for bit (every result
-        // is the reduced representative).  RNG order as the reference's plan:
-        // u, v, w (expr/cache.hpp:226-271).
-        int rc = run_transform(ctx, q, n, batch, false, producer_cbd, 1, 0, nullptr, u);
+        // in its first group, and p*NTT(w) one of p*w.  The three transforms
+        // (u, p*v + lift(m), p*w) share every constant after their first
+        // group, so they run stacked: three first-group launches, then the
+        // other groups once over 3 * batch polynomials.  Two one-product
+        // combines finish; every result is the reduced representative, so the
+        // ciphertext is the reference's bit for bit.  RNG order as the
+        // reference's plan: u, v, w (expr/cache.hpp:226-271).
+        int rc = HMPC_OK;
         const uint32_t* coefficients = plaintext;
-        if (!rc && plaintext_ntt)
+        if (plaintext_ntt)
         {
             rc = run_transform(ctx, p, n, batch, true, producer_tensor, 0, 0, plaintext, coeff);
             coefficients = coeff;
         }
-        TcSmallInput with_msg{coefficients, p};
+        const TcSmallInput with_msg{coefficients, p};
+        const TcSmallInput no_msg{nullptr, p};
+        TcStackPart parts[3];
+        parts[0].vx2 = 1;
+        parts[1].vx2 = 20;
+        parts[1].small = &with_msg;
+        parts[2].vx2 = 20;
+        parts[2].small = &no_msg;
+        uint32_t* stacked = ws;  // [L][3 * elements]: u | p*v + lift(m) | p*w, in NTT form
         if (!rc)
         {
-            rc = run_tc_transform(ctx, q, n, batch, false, producer_cbd, 20, nullptr, v, tc_splits, &with_msg);
+            rc = run_tc_stacked(ctx, q, n, batch, parts, 3, stacked, tc_splits);
         }
-        if (!rc)
+        for (int i = 0; i < 2 && !rc; ++i)
         {
-            cudaError_t e = q->kt->lhe_combine_sum(c0, key_a, n, u, v, elements, q->h, ctx->stream);
-            if (e != cudaSuccess)
-            {
-                return cuda_fail(e, "launching combine");
-            }
-            ++ctx->launches;
-            TcSmallInput no_msg{nullptr, p};
-            rc = run_tc_transform(ctx, q, n, batch, false, producer_cbd, 20, nullptr, v, tc_splits, &no_msg);
-        }
-        if (!rc)
-        {
-            cudaError_t e = q->kt->lhe_combine_sum(c1, key_b, n, u, v, elements, q->h, ctx->stream);
+            cudaError_t e = q->kt->lhe_combine_sum(i ? c1 : c0, i ? key_b : key_a, n, stacked,
+                                                   stacked + (i + 1) * elements, elements, 3 * elements, q->h,
+                                                   ctx->stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching combine");

@@ -78,8 +78,8 @@ namespace hmpc_gb300
         int (*ntt_batched_blocks_per_sm)(int radix_bits, size_t smem);
         int radix_bits;
         cudaError_t (*lhe_combine_sum)(uint32_t* out, const uint32_t* k, uint64_t n, const uint32_t* u,
-                                       const uint32_t* x, uint64_t elements, const HostModulus& m,
-                                       cudaStream_t stream);
+                                       const uint32_t* x, uint64_t elements, uint64_t in_stride,
+                                       const HostModulus& m, cudaStream_t stream);
     };
 
     // sizes of one tensor-core group kernel instantiation (TcShape)

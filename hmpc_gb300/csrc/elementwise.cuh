@@ -171,19 +171,21 @@ namespace hmpc_gb300
     // out = k * u + x with k one polynomial broadcast over the batch: the BGV
     // combine when p * v (+ the lifted plaintext) already went through the
     // transform as one input (linearity of the NTT)
+    // (u and x with plane stride in_stride: parts of a stacked transform output)
     template<int L>
     __global__ void __launch_bounds__(256) lhe_combine_sum_kernel(uint32_t* out, const uint32_t* k, uint64_t n,
                                                                   const uint32_t* u, const uint32_t* x,
-                                                                  uint64_t elements, const Modulus<L> m)
+                                                                  uint64_t elements, uint64_t in_stride,
+                                                                  const Modulus<L> m)
     {
         for (uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < elements;
              e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
         {
             uint32_t a[L], b[L], r[L];
             load1<L>(a, k, n, e % n);
-            load1<L>(b, u, elements, e);
+            load1<L>(b, u, in_stride, e);
             mont_mul<L>(r, a, b, m);
-            load1<L>(a, x, elements, e);
+            load1<L>(a, x, in_stride, e);
             mod_add<L>(r, r, a, m);
             store1<L>(out, elements, e, r);
         }

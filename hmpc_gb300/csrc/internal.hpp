@@ -236,5 +236,18 @@ namespace hmpc_gb300::detail
                          const TcSmallInput* small = nullptr);
     // the tensor-core plan of (n, batch, forward) if one is set for the modulus: splits, else 0
     int tc_plan_splits(hmpc_modulus* mod, uint64_t n, uint64_t batch);
+    // Forward transforms of `count` batches fed by CBD(V) samples (optionally
+    // as p * sample + lift(m)) that share every constant past their first
+    // group: one first-group launch per part into its slice of one digit
+    // buffer, then the remaining groups once over count * batch polynomials.
+    // Part j draws with the context nonce advanced by j * n * batch; out holds
+    // the parts' results side by side (plane stride count * n * batch).
+    struct TcStackPart
+    {
+        uint32_t vx2 = 0;
+        const TcSmallInput* small = nullptr;  // nullptr: plain CBD(V) input
+    };
+    int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
+                       int count, uint32_t* out, int splits);
     int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out);
 }

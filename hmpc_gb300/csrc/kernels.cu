@@ -351,14 +351,15 @@ namespace hmpc_gb300
         }
 
         cudaError_t lhe_combine_sum(uint32_t* out, const uint32_t* kp, uint64_t n, const uint32_t* u,
-                                    const uint32_t* x, uint64_t elements, const HostModulus& h, cudaStream_t stream)
+                                    const uint32_t* x, uint64_t elements, uint64_t in_stride, const HostModulus& h,
+                                    cudaStream_t stream)
         {
             if (elements == 0)
             {
                 return cudaSuccess;
             }
             lhe_combine_sum_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, kp, n, u, x, elements,
-                                                                                  device_modulus(h));
+                                                                                  in_stride, device_modulus(h));
             return cudaGetLastError();
         }
 

@@ -259,6 +259,95 @@ namespace hmpc_gb300::detail
         return log_n >= 4 && !poly_rng && (kind == producer_tensor || kind == producer_cbd) && tc_supported(mod);
     }
 
+    // launch state shared by the groups of one transform (or one stack of them)
+    struct TcLaunch
+    {
+        hmpc_context* ctx;
+        hmpc_modulus* mod;
+        const TcKernels* k;
+        TcTables* tt;
+        uint32_t log_n;
+        float inv_q_top;
+
+        int init(hmpc_context* c, hmpc_modulus* m, uint64_t n, TcTables* t)
+        {
+            ctx = c;
+            mod = m;
+            k = kernels_of(m);
+            tt = t;
+            log_n = static_cast<uint32_t>(__builtin_ctzll(n));
+            const int L = m->c.limbs;
+            // 2^(32(L-1)) / q from the top two limbs
+            const double top = static_cast<double>(m->c.q[static_cast<size_t>(L - 1)]) +
+                               static_cast<double>(m->c.q[static_cast<size_t>(L - 2)]) / 4294967296.0;
+            inv_q_top = static_cast<float>(1.0 / top);
+            if (!ctx->tc_error)
+            {
+                HMPC_CUDA(cudaMalloc(&ctx->tc_error, sizeof(uint32_t)), "allocating the error word");
+                HMPC_CUDA(cudaMemsetAsync(ctx->tc_error, 0, sizeof(uint32_t), ctx->stream), "clearing the error word");
+            }
+            if (!ctx->sm_count)
+            {
+                HMPC_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device),
+                          "querying the SM count");
+            }
+            return HMPC_OK;
+        }
+
+        // group j over `batch` polynomials; stride = plane stride of the digit / limb planes
+        int group(size_t j, const uint32_t* in, uint32_t* out, uint64_t stride, uint64_t batch, int in_kind,
+                  uint32_t vx2, const TcSmallInput* small, uint64_t msg_stride)
+        {
+            const TcGroupPlan& gp = tt->groups[j];
+            const bool first_sampled = j == 0 && (in_kind == tc_in_cbd || in_kind == tc_in_small);
+            TcGroupParams p{};
+            p.in = in;
+            p.out = out;
+            p.images = first_sampled ? (in_kind == tc_in_small ? tt->first_small : tt->first_cbd)
+                                     : tt->images + gp.offset;
+            p.error = ctx->tc_error;
+            p.elements = stride;
+            p.rows = batch << gp.lo;
+            p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
+            p.tiles = gp.blocks * gp.shape.splits * p.tiles_per_block;
+            p.log_n = log_n;
+            p.lo = gp.lo;
+            p.spin_limit = tc_spin_limit;
+            p.rng = ctx->rng();
+            p.vx2 = vx2;
+            p.nw = (2 * vx2 + 31) / 32;
+            for (int i = 0; i < mod->c.limbs; ++i)
+            {
+                p.q[i] = mod->c.q[static_cast<size_t>(i)];
+            }
+            p.inv_q_top = inv_q_top;
+            p.block_shift = tt->groups.back().g;  // the last group's elements per row
+            if (small)
+            {
+                const hmpc_modulus* pm = small->p;
+                p.msg = small->msg;
+                p.msg_stride = msg_stride;
+                p.msg_limbs = static_cast<uint32_t>(pm->c.limbs);
+                p.pninv = pm->c.ninv;
+                for (int i = 0; i < pm->c.limbs; ++i)
+                {
+                    p.pq[i] = pm->c.q[static_cast<size_t>(i)];
+                    p.phalf[i] = pm->c.half[static_cast<size_t>(i)];
+                }
+            }
+            const unsigned grid =
+                static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
+            const int splits = first_sampled ? 1 : static_cast<int>(gp.shape.splits);
+            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, gp.layout, grid, ctx->stream);
+            if (e != cudaSuccess)
+            {
+                return cuda_fail(e, "launching a tensor-core transform group");
+            }
+            ++ctx->launches;
+            return HMPC_OK;
+        }
+    };
+
     int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                          uint32_t vx2, const uint32_t* src, uint32_t* out, int splits, const TcSmallInput* small)
     {
@@ -280,86 +369,103 @@ namespace hmpc_gb300::detail
         {
             return rc;
         }
-        const TcKernels* k = kernels_of(mod);
-        const int L = mod->c.limbs;
         const uint64_t elements = n * batch;
-        const uint32_t w = tt->groups.front().shape.w_out;
+        const uint64_t w = tt->groups.front().shape.w_out;
         const size_t stages = tt->groups.size();
         uint32_t* digits = nullptr;
         if (stages > 1)
         {
-            digits = ctx->tc_scratch((stages > 2 ? 2 : 1) * static_cast<uint64_t>(w) * elements);
+            digits = ctx->tc_scratch((stages > 2 ? 2 : 1) * w * elements);
             if (!digits)
             {
                 return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core digit buffers");
             }
         }
-        if (!ctx->tc_error)
+        TcLaunch run;
+        if (int rc = run.init(ctx, mod, n, tt))
         {
-            HMPC_CUDA(cudaMalloc(&ctx->tc_error, sizeof(uint32_t)), "allocating the error word");
-            HMPC_CUDA(cudaMemsetAsync(ctx->tc_error, 0, sizeof(uint32_t), ctx->stream), "clearing the error word");
+            return rc;
         }
-        if (!ctx->sm_count)
-        {
-            HMPC_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device),
-                      "querying the SM count");
-        }
-        // 2^(32(L-1)) / q from the top two limbs
-        const double top = static_cast<double>(mod->c.q[static_cast<size_t>(L - 1)]) +
-                           static_cast<double>(mod->c.q[static_cast<size_t>(L - 2)]) / 4294967296.0;
-        const float inv_q_top = static_cast<float>(1.0 / top);
-        const RngKey rng = ctx->rng();
+        const int first_kind = cbd ? (small ? tc_in_small : tc_in_cbd) : tc_in_limbs;
         for (size_t j = 0; j < stages; ++j)
         {
-            const TcGroupPlan& gp = tt->groups[j];
-            TcGroupParams p{};
-            p.in = j == 0 ? src : digits + (((j - 1) & 1u) ? static_cast<uint64_t>(w) * elements : 0);
-            p.out = j + 1 == stages ? out : digits + ((j & 1u) ? static_cast<uint64_t>(w) * elements : 0);
-            p.images = (j == 0 && cbd) ? (small ? tt->first_small : tt->first_cbd) : tt->images + gp.offset;
-            p.error = ctx->tc_error;
-            p.elements = elements;
-            p.rows = batch << gp.lo;
-            p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
-            p.tiles = gp.blocks * gp.shape.splits * p.tiles_per_block;
-            p.log_n = static_cast<uint32_t>(__builtin_ctzll(n));
-            p.lo = gp.lo;
-            p.spin_limit = tc_spin_limit;
-            p.rng = rng;
-            p.vx2 = vx2;
-            p.nw = (2 * vx2 + 31) / 32;
-            for (int i = 0; i < L; ++i)
+            const uint32_t* in = j == 0 ? src : digits + (((j - 1) & 1u) ? w * elements : 0);
+            uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * elements : 0);
+            if (int rc = run.group(j, in, o, elements, batch, j == 0 ? first_kind : tc_in_digits, vx2,
+                                   j == 0 ? small : nullptr, elements))
             {
-                p.q[i] = mod->c.q[static_cast<size_t>(i)];
+                return rc;
             }
-            p.inv_q_top = inv_q_top;
-            p.block_shift = tt->groups.back().g;  // the last group's elements per row
-            if (small)
-            {
-                const hmpc_modulus* pm = small->p;
-                p.msg = small->msg;
-                p.msg_limbs = static_cast<uint32_t>(pm->c.limbs);
-                p.pninv = pm->c.ninv;
-                for (int i = 0; i < pm->c.limbs; ++i)
-                {
-                    p.pq[i] = pm->c.q[static_cast<size_t>(i)];
-                    p.phalf[i] = pm->c.half[static_cast<size_t>(i)];
-                }
-            }
-            const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
-            const int in_kind = j == 0 ? (cbd ? static_cast<int>(small ? tc_in_small : tc_in_cbd)
-                                              : static_cast<int>(tc_in_limbs))
-                                       : static_cast<int>(tc_in_digits);
-            const int splits = (j == 0 && cbd) ? 1 : static_cast<int>(gp.shape.splits);
-            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, gp.layout, grid, ctx->stream);
-            if (e != cudaSuccess)
-            {
-                return cuda_fail(e, "launching a tensor-core transform group");
-            }
-            ++ctx->launches;
         }
         if (cbd)
         {
             nonce_add(ctx->nonce, elements);
+        }
+        return HMPC_OK;
+    }
+
+    int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
+                       int count, uint32_t* out, int splits)
+    {
+        bool need_cbd = false, need_small = false;
+        for (int i = 0; i < count; ++i)
+        {
+            if (parts[i].vx2 < 1 || parts[i].vx2 > 64)
+            {
+                return fail(HMPC_ERROR_UNSUPPORTED, "centred binomial needs 1 <= 2V <= 64");
+            }
+            if (parts[i].small && (!parts[i].small->p || parts[i].small->p->c.limbs > 2))
+            {
+                return fail(HMPC_ERROR_UNSUPPORTED, "the small-integer first group needs p < 2^64");
+            }
+            (parts[i].small ? need_small : need_cbd) = true;
+        }
+        if (splits != 1 && splits != 2)
+        {
+            splits = 1;
+        }
+        TcTables* tt = nullptr;
+        if (int rc = prepare_tc(ctx, mod, n, false, splits, need_cbd, need_small, &tt))
+        {
+            return rc;
+        }
+        const uint64_t elements = n * batch;
+        const uint64_t total = elements * static_cast<uint64_t>(count);
+        const uint64_t w = tt->groups.front().shape.w_out;
+        const size_t stages = tt->groups.size();
+        uint32_t* digits = ctx->tc_scratch((stages > 2 ? 2 : 1) * w * total);
+        if (!digits)
+        {
+            return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core digit buffers");
+        }
+        TcLaunch run;
+        if (int rc = run.init(ctx, mod, n, tt))
+        {
+            return rc;
+        }
+        // first groups: part i into its slice of buffer 0 (plane-major slices,
+        // or whole blocked runs when the next group is the last)
+        const bool blocked = (tt->groups.front().layout & 2) != 0;
+        for (int i = 0; i < count; ++i)
+        {
+            uint32_t* slice = digits + static_cast<uint64_t>(i) * elements * (blocked ? w : 1);
+            const int kind = parts[i].small ? tc_in_small : tc_in_cbd;
+            if (int rc = run.group(0, nullptr, stages == 1 ? out + static_cast<uint64_t>(i) * elements : slice, total,
+                                   batch, kind, parts[i].vx2, parts[i].small, elements))
+            {
+                return rc;
+            }
+            nonce_add(ctx->nonce, elements);
+        }
+        // the shared groups over the stacked batch
+        for (size_t j = 1; j < stages; ++j)
+        {
+            const uint32_t* in = digits + (((j - 1) & 1u) ? w * total : 0);
+            uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * total : 0);
+            if (int rc = run.group(j, in, o, total, batch * static_cast<uint64_t>(count), tc_in_digits, 0, nullptr, 0))
+            {
+                return rc;
+            }
         }
         return HMPC_OK;
     }

@@ -95,13 +95,15 @@ namespace hmpc_gb300
         // small-integer loader: plaintext residues mod p (msg_limbs planes of
         // `elements` words, Montgomery form; nullptr: none) and p's constants
         const uint32_t* msg;
+        uint64_t msg_stride;       // plane stride of msg
         uint32_t msg_limbs;
         uint32_t pq[2];
         uint32_t pninv;
         uint32_t phalf[2];
     };
 
-    // balanced base-256 digits of the small-integer input (|x| < 2^70 for p < 2^64, 2V <= 64)
+    // base-256 digits of the small-integer input (|x| < 2^70 for p < 2^64, 2V <= 64):
+    // eight unsigned low bytes and the signed remainder
     constexpr int tc_small_digits = 9;
 
     // Sizes of one group kernel.  NS splits a block's R output elements over
@@ -321,9 +323,10 @@ namespace hmpc_gb300
     // index of the first element, first draw for m, second for m + 4
     // (number_theoretic_transform.hpp:316-329, comp/queue.hpp:191-212); thread
     // (row, part) draws the pair m = part
-    __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t row,
-                                                 uint32_t part)
+    __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t tid)
     {
+        // the four threads of a row are adjacent lanes: a warp's stores cover eight whole segment rows
+        const uint32_t row = tid >> 2, part = tid & 3u;
         const TcRow r = tc_row<3>(p, 0, mt, row);
         int e_u = 0, e_v = 0;
         if (r.ok)
@@ -365,7 +368,7 @@ namespace hmpc_gb300
     __device__ __forceinline__ long long tc_centred_lift(const TcGroupParams& p, uint64_t e)
     {
         const int lp = static_cast<int>(p.msg_limbs);
-        uint32_t t[5] = {p.msg[e], lp > 1 ? p.msg[p.elements + e] : 0u, 0u, 0u, 0u};
+        uint32_t t[5] = {p.msg[e], lp > 1 ? p.msg[p.msg_stride + e] : 0u, 0u, 0u, 0u};
         // word-by-word Montgomery reduction by 2^(32 lp) (core/num/modulo.hpp:30-66)
         for (int i = 0; i < lp; ++i)
         {
@@ -397,10 +400,11 @@ namespace hmpc_gb300
     // first forward group fed by x = p * e + lift(m): e drawn as the CBD
     // loader draws it (one generator per stage-0 pair, thread (row, part) draws
     // the pair m = part, m + 4), m the plaintext residue of the same element;
-    // x is written as 9 balanced base-256 digits (K index = a * 8 + m)
-    __device__ __forceinline__ void tc_store_small(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t row,
-                                                   uint32_t part)
+    // x (|x| < 2^70) is written as its 8 low bytes (unsigned digits) and the
+    // signed value x >> 64 (K index = a * 8 + m)
+    __device__ __forceinline__ void tc_store_small(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t tid)
     {
+        const uint32_t row = tid >> 2, part = tid & 3u;
         const TcRow r = tc_row<3>(p, 0, mt, row);
         __int128 x[2] = {0, 0};
         if (r.ok)
@@ -437,13 +441,14 @@ namespace hmpc_gb300
             }
         }
 #pragma unroll
-        for (int d = 0; d < tc_small_digits; ++d)
+        for (int j = 0; j < 2; ++j)
         {
+            const uint64_t lo = static_cast<uint64_t>(x[j]);
+            const int hi = static_cast<int>(static_cast<long long>(x[j] >> 64));
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
+            for (int d = 0; d < tc_small_digits; ++d)
             {
-                const int digit = static_cast<int>(static_cast<uint32_t>(x[j] + 128) & 255u) - 128;
-                x[j] = (x[j] - digit) >> 8;
+                const int digit = d < 8 ? static_cast<int>((lo >> (8 * d)) & 255u) : hi;
                 const __half h = __int2half_rn(digit);
                 st_shared_u16(sa + tc::operand_offset(row, d * 8 + part + 4 * j, tc_rows),
                               *reinterpret_cast<const uint16_t*>(&h));
@@ -886,7 +891,6 @@ namespace hmpc_gb300
         else
         {
             // ------------------------------------------------ workers
-            const uint32_t row = tid & (tc_rows - 1), part = tid / tc_rows;
             constexpr bool in_blk = (Lay & 1) != 0;
             static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
             TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk> loader;
@@ -919,11 +923,11 @@ namespace hmpc_gb300
                     }
                     if constexpr (IN == tc_in_cbd)
                     {
-                        tc_store_cbd(p, sa, cur.mt, row, part);
+                        tc_store_cbd(p, sa, cur.mt, tid);
                     }
                     else if constexpr (IN == tc_in_small)
                     {
-                        tc_store_small(p, sa, cur.mt, row, part);
+                        tc_store_small(p, sa, cur.mt, tid);
                     }
                     else
                     {
