@@ -453,6 +453,7 @@ def main():
     # modulus): the forward transforms mod q, the inverse one mod p
     q.tune(N, BATCH)
     p.tune(N, BATCH, inverse=True)
+    q.tune(N, 1)  # key generation's single-polynomial transforms
     queue.nonce = [0, 0, 0]
     s0, key0 = lhe.keygen(queue, q, p, N)
     msgs = queue.uniform(p, (BATCH,), N)
