@@ -273,9 +273,10 @@ def dominant_roofline(q, transform_ms, per_transform, int_peak):
 
 def secondary_metrics(queue, int_peak):
     """The other configurations' measurements (parity is in tests/): FMA over
-    2^24 residues (HBM-bound), one N=4096 NTT+INTT (latency), and the batched
+    2^24 residues (HBM-bound), one N=4096 NTT+INTT (latency), the batched
     uneven-degree NTT (512 polynomials, q 192-bit) against one plain call per
-    polynomial."""
+    polynomial, the serving stream, and packing a batch's ciphertexts into
+    network messages (HBM-bound copy)."""
     import torch
 
     from hmpc_gb300.batch import NttBatch, uneven_degrees
@@ -389,6 +390,39 @@ def secondary_metrics(queue, int_peak):
                              "completed": st["completed"], "rejected": st["rejected"], "launches": st["launches"]}
         out[f"serving_poisson_{int(rate)}"] = serving
         del shapes, keys
+
+    # wire format: the 256 ciphertexts of a batch as 512 per-polynomial
+    # messages (1 MiB payloads cut from the batch tensors' limb planes)
+    from hmpc_gb300 import wire
+
+    qw = queue.modulus(Q_256)
+    parts = [queue.uniform(qw, (BATCH,), N) for _ in range(2)]
+    metas, payloads = [], []
+    for i in range(BATCH):
+        for j, part in enumerate(parts):
+            metas.append({"kind": wire.SEND, "sender": 0, "receiver": 1, "id": 2 * i + j + 1})
+            payloads.append(wire.polynomial(part, i))
+    buf, offsets, sizes = wire.pack(queue, metas, payloads)
+    arr = wire._messages(metas, payloads)
+    import ctypes as _ct
+    offs = (_ct.c_uint64 * len(metas))(*offsets)
+    from hmpc_gb300 import _lib as _l
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        _l.call("hmpc_wire_pack", queue.handle, arr, len(metas), 0, None, offs, buf.data_ptr())
+    reps = 10
+    t0.record(stream)
+    for _ in range(reps):
+        _l.call("hmpc_wire_pack", queue.handle, arr, len(metas), 0, None, offs, buf.data_ptr())
+    t1.record(stream)
+    t1.synchronize()
+    ms = t0.elapsed_time(t1) / reps
+    moved = 2 * sum(sizes)
+    hbm, src = hbm_peak_gbs()
+    out["wire_pack_512_messages_1MiB"] = {"ms": ms, "GB/s": moved / (ms * 1e-3) / 1e9,
+                                          "hbm_frac": moved / (ms * 1e-3) / 1e9 / hbm, "hbm_peak_source": src,
+                                          "bytes_read_plus_written": moved}
+    del parts, buf
     return out
 
 

@@ -35,6 +35,20 @@ class TcCost(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_uint32), ("bytes", ctypes.c_double), ("flops", ctypes.c_double)]
 
 
+class WireMessage(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_uint8),
+        ("datatype", ctypes.c_uint8),
+        ("sender", ctypes.c_uint16),
+        ("receiver", ctypes.c_uint16),
+        ("id", ctypes.c_uint64),
+        ("payload", ctypes.c_void_p),
+        ("bytes", ctypes.c_uint64),
+        ("planes", ctypes.c_uint32),
+        ("plane_stride", ctypes.c_uint64),
+    ]
+
+
 class Producer(ctypes.Structure):
     _fields_ = [
         ("kind", ctypes.c_int),
@@ -68,6 +82,16 @@ SIGNATURES = {
     "hmpc_modulus_set_plan": ([_vp, _u64, _u64, _int, _int, _int, _int], _int),
     "hmpc_modulus_get_plan": ([_vp, _u64, _u64, _int] + [ctypes.POINTER(_int)] * 3, _int),
     "hmpc_modulus_tc_cost": ([_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(TcCost)], _int),
+    "hmpc_wire_layout": ([ctypes.POINTER(WireMessage), _u64, ctypes.c_uint8, ctypes.POINTER(_u64),
+                          ctypes.POINTER(_u64)], _int),
+    "hmpc_wire_pack": ([_vp, ctypes.POINTER(WireMessage), _u64, ctypes.c_uint8, ctypes.c_char_p,
+                        ctypes.POINTER(_u64), _vp], _int),
+    "hmpc_wire_unpack": ([_vp, _vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64), _u64, ctypes.c_uint8,
+                          ctypes.c_char_p, ctypes.POINTER(WireMessage), ctypes.POINTER(_vp), _vp], _int),
+    "hmpc_wire_message_id": ([ctypes.c_uint8, ctypes.c_uint8, ctypes.POINTER(ctypes.c_uint16), _int,
+                              ctypes.POINTER(ctypes.c_uint16), _int, ctypes.POINTER(ctypes.c_uint16), _int, _u64,
+                              ctypes.POINTER(_u64)], _int),
+    "hmpc_wire_sha256": ([ctypes.c_char_p, _u64, ctypes.c_char_p], _int),
     "hmpc_modulus_tune": ([_vp, _u64, _u64, _int, ctypes.POINTER(ctypes.c_float)], _int),
     "hmpc_modulus_twiddles": ([_vp, _u64, _int, _u32p], _int),
     "hmpc_tensor_alloc": ([_vp, _u64, ctypes.POINTER(_vp)], _int),

@@ -351,6 +351,72 @@ int hmpc_server_drain(hmpc_server* server, uint32_t timeout_ms);
 int hmpc_server_get_stats(hmpc_server* server, hmpc_server_stats* out);
 int hmpc_server_destroy(hmpc_server* server);
 
+/* ------------------------------------------------------------------ wire
+ * Messages of hmpc's network layer (hmpc-rs/src/net.rs:205-400,
+ * docs/networking.md "Message Format", format version 0), packed and unpacked
+ * on the device; the payload of a tensor is its limb-planar storage
+ * (hmpc/net/queue.hpp:60-88).  No counterpart in the reference's device code:
+ * it serialises on the host from a host accessor.  Header, little-endian:
+ * version u8 = 0, feature flags u8 (bit 0 sessions: a 16-byte session id
+ * follows the header; bit 1 signing: not supported), kind u8 (send 1 ..
+ * all-to-all 6, consistency checks | 0x10), datatype u8 (bit width | 1 for
+ * little-endian: 0x21 for 32-bit limbs), sender u16, receiver u16, message id
+ * u64. */
+#define HMPC_WIRE_SEND 1
+#define HMPC_WIRE_BROADCAST 2
+#define HMPC_WIRE_SCATTER 3
+#define HMPC_WIRE_GATHER 4
+#define HMPC_WIRE_ALL_GATHER 5
+#define HMPC_WIRE_ALL_TO_ALL 6
+#define HMPC_WIRE_FLAG_SESSIONS 1
+#define HMPC_WIRE_FLAG_SIGNING 2
+#define HMPC_WIRE_DATATYPE_U32 0x21
+
+typedef struct hmpc_wire_message
+{
+    uint8_t kind;
+    uint8_t datatype;
+    uint16_t sender;
+    uint16_t receiver;
+    uint64_t id;
+    const void* payload;   /* device memory (pack: read; unpack: ignored) */
+    uint64_t bytes;        /* payload bytes */
+    uint32_t planes;       /* 0 or 1: contiguous; else the payload is `planes` equal parts of a */
+    uint64_t plane_stride; /* multiple of 16 bytes, plane_stride bytes apart in the tensor (one */
+                           /* polynomial's limb planes inside a batch tensor; unpack: the destination) */
+} hmpc_wire_message;
+
+/* Byte offset of each message in a packed buffer (slots start on 16-byte
+ * boundaries, header + payload) and the buffer's size. */
+int hmpc_wire_layout(const hmpc_wire_message* messages, uint64_t count, uint8_t flags, uint64_t* offsets,
+                     uint64_t* total_bytes);
+/* Write `count` messages (header + payload) into device buffer `out` at
+ * `offsets` in one launch on the context's stream. */
+int hmpc_wire_pack(hmpc_context* ctx, const hmpc_wire_message* messages, uint64_t count, uint8_t flags,
+                   const uint8_t session[16], const uint64_t* offsets, uint8_t* out);
+/* Check each received message (device buffer `in`, message i at offsets[i],
+ * sizes[i] bytes) against `expected` (kind, datatype, sender, receiver, id,
+ * payload bytes; version 0, `flags`, the session id) and copy the payloads of
+ * those that match into payloads[i] (device).  status (device, one word per
+ * message) receives 0 or the first mismatching field: 1 version, 2 flags,
+ * 3 kind, 4 datatype, 5 sender, 6 receiver, 7 id, 8 session, 9 size.
+ * Returns when the copies are complete. */
+int hmpc_wire_unpack(hmpc_context* ctx, const uint8_t* in, const uint64_t* offsets, const uint64_t* sizes,
+                     uint64_t count, uint8_t flags, const uint8_t session[16], const hmpc_wire_message* expected,
+                     void* const* payloads, uint32_t* status);
+/* Message id of an operation (hmpc-rs/src/net/queue.rs:108-135): the first
+ * eight bytes, little-endian, of SHA-256(senders || kind || datatype ||
+ * member || receivers) plus `counter` (1 for the first operation with that
+ * hash, then 2, ...); a communicator hashes as its size (u64) and its distinct
+ * party ids (u16) ascending; `member` is the sender (broadcast) or receiver
+ * (gather), none (members = 0) for all-gather and all-to-all. */
+int hmpc_wire_message_id(uint8_t kind, uint8_t datatype, const uint16_t* member, int members,
+                         const uint16_t* senders, int sender_count, const uint16_t* receivers, int receiver_count,
+                         uint64_t counter, uint64_t* id);
+/* SHA-256 of host bytes (FIPS 180-4), as the message id and the signing
+ * feature's payload hash use it. */
+int hmpc_wire_sha256(const void* data, uint64_t bytes, uint8_t digest[32]);
+
 #ifdef __cplusplus
 }
 #endif
