@@ -1087,9 +1087,9 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
         // in its first group, and p*NTT(w) one of p*w.  The three transforms
         // (u, p*v + lift(m), p*w) share every constant after their first
         // group, so they run stacked: three first-group launches, then the
-        // other groups once over 3 * batch polynomials.  Two one-product
-        // combines finish; every result is the reduced representative, so the
-        // ciphertext is the reference's bit for bit.  RNG order as the
+        // other groups once over 3 * batch polynomials.  One combine reads u
+        // once and writes c0 and c1; every result is the reduced
+        // representative, so the ciphertext is the reference's bit for bit.  RNG order as the
         // reference's plan: u, v, w (expr/cache.hpp:226-271).
         int rc = HMPC_OK;
         const uint32_t* coefficients = plaintext;
@@ -1111,11 +1111,9 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
         {
             rc = run_tc_stacked(ctx, q, n, batch, parts, 3, stacked, tc_splits);
         }
-        for (int i = 0; i < 2 && !rc; ++i)
+        if (!rc)
         {
-            cudaError_t e = q->kt->lhe_combine_sum(i ? c1 : c0, i ? key_b : key_a, n, stacked,
-                                                   stacked + (i + 1) * elements, elements, 3 * elements, q->h,
-                                                   ctx->stream);
+            cudaError_t e = q->kt->lhe_combine_pair(c0, c1, key_a, key_b, n, stacked, elements, q->h, ctx->stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching combine");

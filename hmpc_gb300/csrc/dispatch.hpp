@@ -77,9 +77,9 @@ namespace hmpc_gb300
                                    size_t smem, cudaStream_t stream);
         int (*ntt_batched_blocks_per_sm)(int radix_bits, size_t smem);
         int radix_bits;
-        cudaError_t (*lhe_combine_sum)(uint32_t* out, const uint32_t* k, uint64_t n, const uint32_t* u,
-                                       const uint32_t* x, uint64_t elements, uint64_t in_stride,
-                                       const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*lhe_combine_pair)(uint32_t* c0, uint32_t* c1, const uint32_t* ka, const uint32_t* kb,
+                                        uint64_t n, const uint32_t* stacked, uint64_t elements,
+                                        const HostModulus& m, cudaStream_t stream);
     };
 
     // sizes of one tensor-core group kernel instantiation (TcShape)

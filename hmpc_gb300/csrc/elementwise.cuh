@@ -168,26 +168,37 @@ namespace hmpc_gb300
         }
     }
 
-    // out = k * u + x with k one polynomial broadcast over the batch: the BGV
-    // combine when p * v (+ the lifted plaintext) already went through the
-    // transform as one input (linearity of the NTT)
-    // (u and x with plane stride in_stride: parts of a stacked transform output)
+    // c0 = a * u + x and c1 = b * u + w with the key polynomials a, b broadcast
+    // over the batch: the BGV combine when p * v (+ the lifted plaintext) and
+    // p * w already went through the transform as inputs of their own
+    // (linearity of the NTT).  u, x, w are the three parts of one stacked
+    // transform output, [L][3 * elements]; u is read once for both products.
+    // One element per thread (about 50 registers at L = 8): enough resident
+    // warps to cover the loads' latency with the products' arithmetic.
+    // n is a power of two.
     template<int L>
-    __global__ void __launch_bounds__(256) lhe_combine_sum_kernel(uint32_t* out, const uint32_t* k, uint64_t n,
-                                                                  const uint32_t* u, const uint32_t* x,
-                                                                  uint64_t elements, uint64_t in_stride,
-                                                                  const Modulus<L> m)
+    __global__ void __launch_bounds__(256) lhe_combine_pair_kernel(uint32_t* c0, uint32_t* c1, const uint32_t* ka,
+                                                                   const uint32_t* kb, uint64_t n,
+                                                                   const uint32_t* stacked, uint64_t elements,
+                                                                   const Modulus<L> m)
     {
+        const uint64_t stride = 3 * elements;
+        const uint64_t mask = n - 1;
         for (uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < elements;
              e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
         {
-            uint32_t a[L], b[L], r[L];
-            load1<L>(a, k, n, e % n);
-            load1<L>(b, u, in_stride, e);
-            mont_mul<L>(r, a, b, m);
-            load1<L>(a, x, in_stride, e);
-            mod_add<L>(r, r, a, m);
-            store1<L>(out, elements, e, r);
+            uint32_t u[L], k[L], x[L];
+            load1<L>(u, stacked, stride, e);
+            load1<L>(k, ka, n, e & mask);
+            load1<L>(x, stacked + elements, stride, e);
+            mont_mul<L>(k, k, u, m);
+            mod_add<L>(x, x, k, m);
+            store1<L>(c0, elements, e, x);
+            load1<L>(k, kb, n, e & mask);
+            load1<L>(x, stacked + 2 * elements, stride, e);
+            mont_mul<L>(k, k, u, m);
+            mod_add<L>(x, x, k, m);
+            store1<L>(c1, elements, e, x);
         }
     }
 

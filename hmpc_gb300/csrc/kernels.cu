@@ -350,22 +350,22 @@ namespace hmpc_gb300
             return e == cudaSuccess ? blocks : 0;
         }
 
-        cudaError_t lhe_combine_sum(uint32_t* out, const uint32_t* kp, uint64_t n, const uint32_t* u,
-                                    const uint32_t* x, uint64_t elements, uint64_t in_stride, const HostModulus& h,
-                                    cudaStream_t stream)
+        cudaError_t lhe_combine_pair(uint32_t* c0, uint32_t* c1, const uint32_t* ka, const uint32_t* kb, uint64_t n,
+                                     const uint32_t* stacked, uint64_t elements, const HostModulus& h,
+                                     cudaStream_t stream)
         {
             if (elements == 0)
             {
                 return cudaSuccess;
             }
-            lhe_combine_sum_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, kp, n, u, x, elements,
-                                                                                  in_stride, device_modulus(h));
+            lhe_combine_pair_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(c0, c1, ka, kb, n, stacked,
+                                                                                   elements, device_modulus(h));
             return cudaGetLastError();
         }
 
         const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd, to_montgomery,
                                    from_montgomery, cast, plain_stage, ct_mul, dec_combine, ntt_batched,
-                                   ntt_batched_blocks_per_sm, R, lhe_combine_sum};
+                                   ntt_batched_blocks_per_sm, R, lhe_combine_pair};
     }
 
     const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()

@@ -365,10 +365,11 @@ namespace hmpc_gb300
     // canonical value of a residue mod p (one or two limbs, Montgomery form),
     // lifted to the centred integer in (-p/2, p/2] (hmpc/ints/mod.hpp:259-307:
     // the canonical value v becomes v - p when v > floor(p/2))
-    __device__ __forceinline__ long long tc_centred_lift(const TcGroupParams& p, uint64_t e)
+    // (m: the residue's limbs as loaded)
+    __device__ __forceinline__ long long tc_centred_lift(const TcGroupParams& p, const uint32_t (&m)[2])
     {
         const int lp = static_cast<int>(p.msg_limbs);
-        uint32_t t[5] = {p.msg[e], lp > 1 ? p.msg[p.msg_stride + e] : 0u, 0u, 0u, 0u};
+        uint32_t t[5] = {m[0], m[1], 0u, 0u, 0u};
         // word-by-word Montgomery reduction by 2^(32 lp) (core/num/modulo.hpp:30-66)
         for (int i = 0; i < lp; ++i)
         {
@@ -412,6 +413,19 @@ namespace hmpc_gb300
             const int count = 2 * static_cast<int>(p.vx2);
             const int nw = static_cast<int>(p.nw);
             const uint64_t idx = r.base + (static_cast<uint64_t>(part) << p.lo);
+            // the plaintext loads go out before the keystream is computed, so
+            // their latency hides behind it
+            uint32_t msg[2][2] = {{0u, 0u}, {0u, 0u}};
+            if (p.msg)
+            {
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                {
+                    const uint64_t e = idx + (static_cast<uint64_t>(4 * j) << p.lo);
+                    msg[j][0] = __ldcs(p.msg + e);
+                    msg[j][1] = p.msg_limbs > 1 ? __ldcs(p.msg + p.msg_stride + e) : 0u;
+                }
+            }
             uint32_t w[8];
             chacha_stream<8>(p.rng, static_cast<uint32_t>(idx), w);
             int a = 0, b = 0;
@@ -436,8 +450,8 @@ namespace hmpc_gb300
             x[1] = static_cast<__int128>(pval) * (b - static_cast<int>(p.vx2));
             if (p.msg)
             {
-                x[0] += tc_centred_lift(p, idx);
-                x[1] += tc_centred_lift(p, idx + (4ull << p.lo));
+                x[0] += tc_centred_lift(p, msg[0]);
+                x[1] += tc_centred_lift(p, msg[1]);
             }
         }
 #pragma unroll
