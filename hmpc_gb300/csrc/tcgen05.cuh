@@ -114,12 +114,39 @@ namespace hmpc_gb300::tc
         return done != 0;
     }
 
+    // as mbar_try_wait, but a thread whose phase is not complete may sleep up
+    // to `ns` nanoseconds (waking when the phase completes) instead of
+    // returning at once: waiting warps leave the issue slots to working ones
+    __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns)
+    {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+            : "memory");
+        return done != 0;
+    }
+
     // bounded wait for the phase `parity` of an mbarrier; false when the limit ran out
     __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit)
     {
         for (uint32_t i = 0; i < limit; ++i)
         {
             if (mbar_try_wait(bar, parity))
+            {
+                return true;
+            }
+        }
+        return false;
+    }
+
+    // bounded wait of at most limit polls of up to 1 us each
+    __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t limit)
+    {
+        for (uint32_t i = 0; i < limit; ++i)
+        {
+            if (mbar_try_wait_sleep(bar, parity, 1000u))
             {
                 return true;
             }

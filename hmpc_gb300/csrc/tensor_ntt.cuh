@@ -927,7 +927,8 @@ namespace hmpc_gb300
                         uint32_t ok = 1;
                         if (lane == 0)
                         {
-                            ok = tc::mbar_wait(bar_a_empty, static_cast<uint32_t>((i - 1) & 1u), p.spin_limit);
+                            ok = tc::mbar_wait_sleep(bar_a_empty, static_cast<uint32_t>((i - 1) & 1u),
+                                                     p.spin_limit);
                         }
                         if (!__shfl_sync(0xffffffffu, ok, 0))
                         {
@@ -965,7 +966,7 @@ namespace hmpc_gb300
                     uint32_t ok = 1;
                     if (lane == 0)
                     {
-                        ok = tc::mbar_wait(&bar_acc_full[acc], static_cast<uint32_t>(((i - 1) >> 1) & 1u),
+                        ok = tc::mbar_wait_sleep(&bar_acc_full[acc], static_cast<uint32_t>(((i - 1) >> 1) & 1u),
                                            p.spin_limit);
                     }
                     if (!__shfl_sync(0xffffffffu, ok, 0))
