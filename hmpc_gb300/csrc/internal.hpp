@@ -51,6 +51,9 @@ namespace hmpc_gb300::detail
         TcShapeInfo cbd_shape;
         uint8_t* first_small = nullptr;  // first group fed by p * sample + lift(plaintext)
         TcShapeInfo small_shape;
+        // false: a group's constants exceed the two-operation carry's range and
+        // this (modulus, degree, direction) runs on the CUDA cores
+        bool fit = true;
     };
 
     // first group of a forward transform fed by x = p * CBD(V) + lift(m):

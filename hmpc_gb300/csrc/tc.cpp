@@ -3,7 +3,10 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cuda_fp16.h>
+
 #include "internal.hpp"
+#include "tcgen05.cuh"
 
 using namespace hmpc_gb300;
 using namespace hmpc_gb300::detail;
@@ -54,6 +57,48 @@ namespace
             groups[groups.size() - 2].layout |= 2;
         }
         return groups;
+    }
+
+    // The carry of a group fed by digits takes two operations per digit while
+    // every column sum stays within (-2^22 + 2^15, 2^22 - 2^15); with digits
+    // |x| <= 128 that holds when each constant column's sum of |digit| is at
+    // most this bound (about twice what balanced random digits give)
+    constexpr uint32_t tc_byte_carry_column_bound = 32512;
+
+    // the largest sum of |digit| over one column (output digit) of a group's images
+    __global__ void tc_column_bound_kernel(const uint8_t* images, uint64_t columns, uint32_t n_mma,
+                                           uint32_t image_bytes, uint32_t k_pad, uint32_t* out)
+    {
+        const uint64_t id = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+        if (id >= columns)
+        {
+            return;
+        }
+        const uint8_t* img = images + (id / n_mma) * image_bytes;
+        const uint32_t n = static_cast<uint32_t>(id % n_mma);
+        float sum = 0.0f;  // at most 288 * 128: exact
+        for (uint32_t k = 0; k < k_pad; ++k)
+        {
+            sum += fabsf(__half2float(*reinterpret_cast<const __half*>(img + tc::operand_offset(n, k, n_mma))));
+        }
+        atomicMax(out, static_cast<uint32_t>(sum));
+    }
+
+    // whether a digit-fed group's constants keep its sums in the carry's range
+    int check_column_bound(hmpc_context* ctx, const TcGroupPlan& gp, const uint8_t* images, uint32_t* d_max,
+                           bool* fit)
+    {
+        const uint64_t columns = gp.blocks * gp.shape.splits * gp.shape.n_mma;
+        HMPC_CUDA(cudaMemsetAsync(d_max, 0, sizeof(uint32_t), ctx->stream), "clearing the column bound");
+        tc_column_bound_kernel<<<static_cast<unsigned>((columns + 255) / 256), 256, 0, ctx->stream>>>(
+            images, columns, gp.shape.n_mma, gp.shape.b_bytes, gp.shape.k_pad, d_max);
+        HMPC_CUDA(cudaGetLastError(), "launching the column bound");
+        uint32_t bound = 0;
+        HMPC_CUDA(cudaMemcpyAsync(&bound, d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream),
+                  "reading the column bound");
+        HMPC_CUDA(cudaStreamSynchronize(ctx->stream), "checking tensor-core constants");
+        *fit = bound <= tc_byte_carry_column_bound;
+        return HMPC_OK;
     }
 
     // generate and expand one group's constants into `images`
@@ -107,6 +152,11 @@ namespace
         auto key = std::make_tuple(log_n, inverse ? 1 : 0, splits);
         auto it = mod->tc_tables.find(key);
         const bool fresh = it == mod->tc_tables.end();
+        if (!fresh && !it->second.fit)
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED,
+                        "this modulus's tensor-core constants exceed the carry's range; use a CUDA-core tile shape");
+        }
         if (!fresh && (!need_cbd || it->second.first_cbd) && (!need_small || it->second.first_small))
         {
             *out = &it->second;
@@ -154,7 +204,7 @@ namespace
             cudaFree(d_pow);
             cudaFree(d_gx);
         };
-        if (cudaMalloc(&d_pow, pow256.size() * sizeof(uint32_t)) != cudaSuccess ||
+        if (cudaMalloc(&d_pow, (pow256.size() + 1) * sizeof(uint32_t)) != cudaSuccess ||
             cudaMalloc(&d_gx, gx_words * sizeof(uint32_t)) != cudaSuccess)
         {
             cleanup();
@@ -185,6 +235,26 @@ namespace
                 }
                 // the generation scratch is reused by the next group
                 cudaStreamSynchronize(ctx->stream);
+                bool fit = true;
+                if (gp.in_kind == tc_in_digits)
+                {
+                    if (int rc = check_column_bound(ctx, gp, tt.images + gp.offset, d_pow + pow256.size(), &fit))
+                    {
+                        cleanup();
+                        cudaFree(tt.images);
+                        return rc;
+                    }
+                }
+                if (!fit)
+                {
+                    cleanup();
+                    cudaFree(tt.images);
+                    TcTables unfit;
+                    unfit.fit = false;
+                    mod->tc_tables[key] = unfit;
+                    return fail(HMPC_ERROR_UNSUPPORTED, "this modulus's tensor-core constants exceed the carry's "
+                                                        "range; use a CUDA-core tile shape");
+                }
             }
         }
         if (need_cbd && !tt.first_cbd)

@@ -499,6 +499,31 @@ namespace hmpc_gb300
         }
     };
 
+    // The same carry in two operations per digit where |t| < 2^22 - 2^15: with
+    // C2 = 2^23 + 2^22 every T = t + C2 lies in [2^23, 2^24), where a float's
+    // mantissa is T - 2^23 exactly, so the low byte of T's bits is t mod 256 --
+    // the biased digit, read from T itself.  The state x = floor(T / 256) +
+    // C2 - C2 / 256 + 128 equals (next carry + 128) + C2, so the next T is s + x.
+    // Sums of a group fed by digits (|x| <= 128) stay in range when every
+    // constant column's sum of |digit| is at most 32512: checked when the
+    // group's constants are built.  Fed by limbs (unsigned bytes) they may not.
+    struct DigitCarryByte
+    {
+        float x = 12583040.0f;  // carry 0: 128 + C2
+
+        __device__ __forceinline__ uint32_t step(float s)
+        {
+            const float t = s + x;                          // t + C2
+            x = __fmaf_rd(t, 0.00390625f, 12533888.0f);     // floor((t + C2) / 256) + C2 - C2 / 256 + 128
+            return __float_as_uint(t);
+        }
+
+        __device__ __forceinline__ int carry() const
+        {
+            return static_cast<int>(__float_as_uint(x) - 0x4B000000u) - 4194432;
+        }
+    };
+
     template<int DC>
     __device__ __forceinline__ void tc_load_sums(uint32_t taddr, uint32_t (&s)[DC])
     {
@@ -580,8 +605,9 @@ namespace hmpc_gb300
 
     // carry the accumulator of one tile out of TMEM: each thread owns one row
     // and `per` consecutive output elements of the block's split; Contig: the
-    // row's elements are adjacent (no column bits), stored as vectors
-    template<int DC, int R, int OUT, int NS, bool Contig, bool OutRec>
+    // row's elements are adjacent (no column bits), stored as vectors;
+    // ByteCarry: the two-operation carry (inputs other than limbs)
+    template<int DC, int R, int OUT, int NS, bool Contig, bool OutRec, bool ByteCarry>
     __device__ __forceinline__ void tc_epilogue(const TcGroupParams& p, uint32_t tmem, const TcCursor& cur,
                                                 uint32_t warp, uint32_t lane)
     {
@@ -611,7 +637,7 @@ namespace hmpc_gb300
             uint32_t s[DC];
             tc_load_sums<DC>(tmem + ((32u * lg) << 16) + (kl0 + kk) * DC, s);
             tc::tmem_load_wait();
-            DigitCarry carry;
+            std::conditional_t<ByteCarry, DigitCarryByte, DigitCarry> carry;
             uint32_t words[W];
             uint32_t bb[4];
 #pragma unroll
@@ -975,7 +1001,8 @@ namespace hmpc_gb300
                         break;
                     }
                     tc::fence_after_sync();
-                    tc_epilogue<DC, R, OUT, NS, Contig, (Lay & 2) != 0>(p, tmem + acc * S::cols, prev, warp, lane);
+                    tc_epilogue<DC, R, OUT, NS, Contig, (Lay & 2) != 0, IN != tc_in_limbs>(p, tmem + acc * S::cols,
+                                                                                          prev, warp, lane);
                     tc::fence_before_sync();
                     mbar_arrive(&bar_acc_empty[acc]);
                 }
