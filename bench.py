@@ -321,6 +321,7 @@ def secondary_metrics(queue, int_peak):
 
     def graphed(fn, reps=200):
         side = torch.cuda.Stream()
+        side.wait_stream(stream)  # the inputs made on the queue's stream
         queue.set_stream(side)
         try:
             with torch.cuda.stream(side):
@@ -466,7 +467,7 @@ def main():
     import torch
     import torch.distributed as dist
 
-    from hmpc_gb300 import lhe
+    from hmpc_gb300 import _lib, lhe
     from hmpc_gb300.comp import Queue, Tensor
 
     torch.cuda.set_device(local)
@@ -478,6 +479,10 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    # one stream of its own for the queue and torch's own work (not the legacy
+    # default stream, which would serialise with the copy streams of the
+    # end-to-end measurement)
+    torch.cuda.set_stream(torch.cuda.Stream(local))
     queue = Queue(key=SEED_KEY, device=local)
     stream = queue.stream
     q, p = queue.modulus(Q_256), queue.modulus(P_64)
@@ -496,10 +501,6 @@ def main():
     key = lhe.Key(Tensor(q, (), N), Tensor(q, (), N))
 
     def step(messages):
-        import ctypes
-
-        from hmpc_gb300 import _lib
-
         _lib.call("hmpc_lhe_keygen", queue.handle, q.handle, p.handle, N, s.ptr(), key.a.ptr(), key.b.ptr())
         lhe.enc(queue, key, messages, q, out=ct)
 
@@ -520,30 +521,58 @@ def main():
     value = whole_job_rate(BATCH, world, args.steps, elapsed_ms)
 
     # ------------------------------------- e2e through the API, host buffers
+    # Every step copies its plaintexts in from pinned host memory, encrypts
+    # and copies both ciphertext halves back, as a serving loop does: the
+    # copies of one step overlap the encryption of the next (a copy-in and a
+    # copy-out stream, two buffer sets; events order the reuse of each set).
+    copy_in, copy_out = torch.cuda.Stream(local), torch.cuda.Stream(local)
     host_msgs = torch.empty(msgs.data.shape, dtype=torch.int32, pin_memory=True)
     host_msgs.copy_(msgs.data.cpu())
-    host_c0 = torch.empty(ct.c0.data.shape, dtype=torch.int32, pin_memory=True)
-    host_c1 = torch.empty(ct.c1.data.shape, dtype=torch.int32, pin_memory=True)
-    dev_msgs = Tensor(p, (BATCH,), N)
+    sets = []
+    for _ in range(2):
+        sets.append({
+            "msgs": Tensor(p, (BATCH,), N),
+            "ct": lhe.Ciphertext(Tensor(q, (BATCH,), N), Tensor(q, (BATCH,), N)),
+            "c0": torch.empty(ct.c0.data.shape, dtype=torch.int32, pin_memory=True),
+            "c1": torch.empty(ct.c1.data.shape, dtype=torch.int32, pin_memory=True),
+            "loaded": torch.cuda.Event(), "done": torch.cuda.Event(), "read": torch.cuda.Event(),
+        })
+    for b in sets:
+        b["read"].record(stream)
+        b["done"].record(stream)
 
-    def e2e_step():
-        with torch.cuda.stream(stream):
-            dev_msgs.data.copy_(host_msgs, non_blocking=True)
-            step(dev_msgs)
-            host_c0.copy_(ct.c0.data, non_blocking=True)
-            host_c1.copy_(ct.c1.data, non_blocking=True)
+    def e2e_step(i):
+        b = sets[i % 2]
+        copy_in.wait_event(b["done"])  # the set's plaintexts are no longer read
+        with torch.cuda.stream(copy_in):
+            b["msgs"].data.copy_(host_msgs, non_blocking=True)
+        b["loaded"].record(copy_in)
+        stream.wait_event(b["loaded"])
+        stream.wait_event(b["read"])  # the set's previous ciphertexts are copied out
+        _lib.call("hmpc_lhe_keygen", queue.handle, q.handle, p.handle, N, s.ptr(), key.a.ptr(), key.b.ptr())
+        lhe.enc(queue, key, b["msgs"], q, out=b["ct"])
+        b["done"].record(stream)
+        copy_out.wait_event(b["done"])
+        with torch.cuda.stream(copy_out):
+            b["c0"].copy_(b["ct"].c0.data, non_blocking=True)
+            b["c1"].copy_(b["ct"].c1.data, non_blocking=True)
+        b["read"].record(copy_out)
 
-    for _ in range(args.warmup):
-        e2e_step()
+    for i in range(args.warmup):
+        e2e_step(i)
     barrier()
     e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e_start.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
+    copy_in.wait_stream(stream)
+    for i in range(args.steps):
+        e2e_step(i)
+    stream.wait_stream(copy_out)
     e_stop.record(stream)
     barrier()
     e2e_ms = max_over_ranks(e_start.elapsed_time(e_stop), world, device="cuda")
     e2e_value = whole_job_rate(BATCH, world, args.steps, e2e_ms)
+    last = sets[(args.steps - 1) % 2]
+    host_c0, host_c1 = last["c0"], last["c1"]
     # check the e2e result once: decrypting the copied-back ciphertext gives the messages
     back = lhe.Ciphertext(Tensor(q, (BATCH,), N, host_c0.to(queue.device)), Tensor(q, (BATCH,), N,
                                                                                host_c1.to(queue.device)))
