@@ -458,6 +458,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--plan", default="tuned", choices=["tuned", "tensor"],
+                    help="tensor: run q's batch transforms on the tensor-core engine (one constant image per "
+                         "block, as the tuner picks on a GB300) instead of timing the candidates -- for captures "
+                         "under a profiler, whose per-launch overhead skews the tuner toward fewer launches")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -490,7 +494,10 @@ def main():
     p.prepare(N)
     # autotune the tile shape (or engine) of the batch's transforms (kept per
     # modulus): the forward transforms mod q, the inverse one mod p
-    q.tune(N, BATCH)
+    if args.plan == "tensor":
+        q.set_plan(N, BATCH, False, radix_bits=0, local_bits=1)
+    else:
+        q.tune(N, BATCH)
     p.tune(N, BATCH, inverse=True)
     q.tune(N, 1)  # key generation's single-polynomial transforms
     queue.nonce = [0, 0, 0]
