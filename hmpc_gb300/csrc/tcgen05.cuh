@@ -141,12 +141,13 @@ namespace hmpc_gb300::tc
         return false;
     }
 
-    // bounded wait of at most limit polls of up to 1 us each
-    __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t limit)
+    // bounded wait of at most limit polls of up to ns nanoseconds each
+    __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t limit,
+                                                    uint32_t ns = 1000u)
     {
         for (uint32_t i = 0; i < limit; ++i)
         {
-            if (mbar_try_wait_sleep(bar, parity, 1000u))
+            if (mbar_try_wait_sleep(bar, parity, ns))
             {
                 return true;
             }

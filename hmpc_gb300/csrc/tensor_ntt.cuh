@@ -877,7 +877,9 @@ namespace hmpc_gb300
                             copy(prev_jb + 2, prev_jb % 2);
                         }
                     }
-                    if (!tc::mbar_wait(bar_a_full, static_cast<uint32_t>(i & 1u), p.spin_limit))
+                    // the longest wait of this thread: sleeping in it leaves the
+                    // issue slots of its sub-partition to the workers
+                    if (!tc::mbar_wait_sleep(bar_a_full, static_cast<uint32_t>(i & 1u), p.spin_limit, 200u))
                     {
                         give_up(4);
                         break;
