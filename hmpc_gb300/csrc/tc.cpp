@@ -129,6 +129,10 @@ namespace
         ex.splits = gp.shape.splits;
         ex.n_mma = gp.shape.n_mma;
         ex.image_bytes = gp.shape.b_bytes;
+        // the loaders of r = 8 groups fed by digits or limbs whose rows are
+        // strided elements (the kernel's contiguous variant runs where lo = 0)
+        // take word-major K
+        ex.word_major = ex.r == 8 && d_in >= ex.dc && gp.lo != 0 ? 1u : 0u;
         for (int j = 0; j < mod->c.limbs; ++j)
         {
             ex.half[j] = mod->c.half[static_cast<size_t>(j)];

@@ -118,7 +118,7 @@ namespace hmpc_gb300
                                     : (IN == tc_in_limbs ? DC : (IN == tc_in_small ? tc_small_digits : 1));
         static constexpr bool generated = IN == tc_in_cbd || IN == tc_in_small;  // no input planes
         static constexpr int w_in = generated ? 0 : (d_in + 3) / 4;
-        // digit slots per element on the K axis (K index = a * R + m)
+        // digit slots per element on the K axis (K index of digit a of element m: tc_k_index)
         static constexpr int d_eff = generated ? d_in : (R == 8 ? d_in : (R == 4 ? (d_in + 1) / 2 * 2 : w_in * 4));
         static constexpr int k_real = R * d_eff;
         static constexpr int k_pad = (k_real + 15) / 16 * 16;
@@ -145,6 +145,29 @@ namespace hmpc_gb300
         const __half2 b = __halves2half2(__float2half(1024.0f + Bias), __float2half(1024.0f + Bias));
         h = __hsub2(h, b);
         return *reinterpret_cast<uint32_t*>(&h);
+    }
+
+    // bytes t and t + 1 of one word -> fp16x2 of (byte - bias): one byte
+    // permute puts them under the exponent byte of 1024
+    template<int Bias>
+    __device__ __forceinline__ uint32_t byte_pair_to_half2(uint32_t x, uint32_t t)
+    {
+        uint32_t y = __byte_perm(x, 0x64646464u, t | (4u << 4) | ((t + 1u) << 8) | (4u << 12));
+        __half2 h = *reinterpret_cast<__half2*>(&y);
+        const __half2 b = __halves2half2(__float2half(1024.0f + Bias), __float2half(1024.0f + Bias));
+        h = __hsub2(h, b);
+        return *reinterpret_cast<uint32_t*>(&h);
+    }
+
+    // K index of digit a of the group's input element i.  Word-major (r = 8
+    // fed by digits or limbs, rows of strided elements): the first DC digits
+    // at (a / 4) * 4r + 4i + a % 4,
+    // so one 16-byte piece holds the four digits of one word of two elements;
+    // otherwise (and for the carry digits past DC) a * r + i
+    __host__ __device__ __forceinline__ uint32_t tc_k_index(uint32_t a, uint32_t i, uint32_t r, uint32_t dc,
+                                                            bool word_major)
+    {
+        return word_major && a < dc ? (a / 4u) * 4u * r + 4u * i + a % 4u : a * r + i;
     }
 
     __device__ __forceinline__ void st_shared_v4(uint8_t* p, uint32_t a, uint32_t b, uint32_t c, uint32_t d)
@@ -201,7 +224,8 @@ namespace hmpc_gb300
     // tc_parts, ... of the row's R elements
     // InBlk: the input digit planes are blocked per R adjacent elements (word w
     // of element e at (e - e mod R) * W + w * R + e mod R): a row is one run
-    template<int DC, int R, int IN, int NS, int Parts, bool InBlk = false>
+    // WordMajor: r = 8 tiles take the word-major K order of tc_k_index
+    template<int DC, int R, int IN, int NS, int Parts, bool InBlk = false, bool WordMajor = false>
     struct TcLoader
     {
         using S = TcShape<DC, R, IN, NS>;
@@ -266,17 +290,34 @@ namespace hmpc_gb300
                 }
                 if constexpr (R == 8)
                 {
-#pragma unroll
-                    for (uint32_t t = 0; t < 4; ++t)
+                    if (WordMajor && w < static_cast<uint32_t>(DC / 4))
                     {
-                        const uint32_t a = 4 * w + t;
-                        if (a < static_cast<uint32_t>(S::d_eff))
+                        // word-major K (tc_k_index): elements 2 mp and 2 mp + 1 per piece
+#pragma unroll
+                        for (uint32_t mp = 0; mp < 4; ++mp)
                         {
-                            st_shared_v4(sa + tc::operand_offset(row, a * 8, tc_rows),
-                                         bytes_to_half2<bias>(v[wi][0], v[wi][1], t),
-                                         bytes_to_half2<bias>(v[wi][2], v[wi][3], t),
-                                         bytes_to_half2<bias>(v[wi][4], v[wi][5], t),
-                                         bytes_to_half2<bias>(v[wi][6], v[wi][7], t));
+                            st_shared_v4(sa + tc::operand_offset(row, 32 * w + 8 * mp, tc_rows),
+                                         byte_pair_to_half2<bias>(v[wi][2 * mp], 0),
+                                         byte_pair_to_half2<bias>(v[wi][2 * mp], 2),
+                                         byte_pair_to_half2<bias>(v[wi][2 * mp + 1], 0),
+                                         byte_pair_to_half2<bias>(v[wi][2 * mp + 1], 2));
+                        }
+                    }
+                    else
+                    {
+                        // K = a * 8 + m (and the carry digits past DC in word-major order)
+#pragma unroll
+                        for (uint32_t t = 0; t < 4; ++t)
+                        {
+                            const uint32_t a = 4 * w + t;
+                            if (a < static_cast<uint32_t>(S::d_eff))
+                            {
+                                st_shared_v4(sa + tc::operand_offset(row, a * 8, tc_rows),
+                                             bytes_to_half2<bias>(v[wi][0], v[wi][1], t),
+                                             bytes_to_half2<bias>(v[wi][2], v[wi][3], t),
+                                             bytes_to_half2<bias>(v[wi][4], v[wi][5], t),
+                                             bytes_to_half2<bias>(v[wi][6], v[wi][7], t));
+                            }
                         }
                     }
                 }
@@ -935,7 +976,9 @@ namespace hmpc_gb300
             // ------------------------------------------------ workers
             constexpr bool in_blk = (Lay & 1) != 0;
             static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
-            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk> loader;
+            // word-major K where rows are columns of strided elements; the
+            // contiguous last group measured faster with digit-major K
+            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig> loader;
             TcCursor cur = first;
             if constexpr (!S::generated)
             {
@@ -1144,11 +1187,12 @@ namespace hmpc_gb300
         uint8_t* images;         // blocks * splits images of image_bytes, zero-filled
         uint64_t blocks;
         uint32_t r, dc, d_in, splits, n_mma, image_bytes;
+        uint32_t word_major;     // K order of the group's loader (tc_k_index)
         uint32_t half[8];        // floor(q / 2)
     };
 
     // Constant digits: output k of block h lives in image h * splits + k / (r /
-    // splits), row (k mod (r / splits)) * DC + b, column a * r + i: balanced
+    // splits), row (k mod (r / splits)) * DC + b, column tc_k_index(a, i): balanced
     // digit b in [-128, 127] of the signed value V = (256^a * G[k][i] mod q)
     // in (-q/2, q/2] (V taken in two's complement; the 4L balanced digits of
     // any |V| <= 0x7F7F..7F are exact).
@@ -1208,8 +1252,9 @@ namespace hmpc_gb300
                 digit = byte - 256;
                 carry = 1;
             }
-            *reinterpret_cast<__half*>(img + tc::operand_offset(k_local * p.dc + b, a * p.r + i, p.n_mma)) =
-                __int2half_rn(digit);
+            *reinterpret_cast<__half*>(img + tc::operand_offset(k_local * p.dc + b,
+                                                                 tc_k_index(a, i, p.r, p.dc, p.word_major != 0),
+                                                                 p.n_mma)) = __int2half_rn(digit);
         }
     }
 }
