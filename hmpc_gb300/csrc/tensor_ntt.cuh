@@ -409,32 +409,29 @@ namespace hmpc_gb300
     // (m: the residue's limbs as loaded)
     __device__ __forceinline__ long long tc_centred_lift(const TcGroupParams& p, const uint32_t (&m)[2])
     {
-        const int lp = static_cast<int>(p.msg_limbs);
-        uint32_t t[5] = {m[0], m[1], 0u, 0u, 0u};
-        // word-by-word Montgomery reduction by 2^(32 lp) (core/num/modulo.hpp:30-66)
-        for (int i = 0; i < lp; ++i)
+        // word-by-word Montgomery reduction by 2^(32 lp) (core/num/modulo.hpp:30-66),
+        // written out for one and two limbs so no scratch array is indexed
+        const bool two = p.msg_limbs > 1;
+        const uint64_t q = p.pq[0] | (two ? static_cast<uint64_t>(p.pq[1]) << 32 : 0ull);
+        const uint64_t half = p.phalf[0] | (two ? static_cast<uint64_t>(p.phalf[1]) << 32 : 0ull);
+        uint64_t v;
+        if (two)
         {
-            const uint32_t mq = t[i] * p.pninv;
-            uint64_t carry = 0;
-            for (int j = 0; j < lp; ++j)
+            unsigned __int128 t = (static_cast<uint64_t>(m[1]) << 32) | m[0];
+            t += static_cast<unsigned __int128>(m[0] * p.pninv) * q;  // low word becomes 0
+            t >>= 32;
+            t += static_cast<unsigned __int128>(static_cast<uint32_t>(t) * p.pninv) * q;
+            t >>= 32;  // < 2q
+            v = static_cast<uint64_t>(t);
+            if ((t >> 64) != 0 || v >= q)
             {
-                const uint64_t s = static_cast<uint64_t>(mq) * p.pq[j] + t[i + j] + carry;
-                t[i + j] = static_cast<uint32_t>(s);
-                carry = s >> 32;
-            }
-            for (int k = i + lp; k < 5; ++k)
-            {
-                const uint64_t s = static_cast<uint64_t>(t[k]) + carry;
-                t[k] = static_cast<uint32_t>(s);
-                carry = s >> 32;
+                v -= q;
             }
         }
-        const uint64_t q = p.pq[0] | (lp > 1 ? static_cast<uint64_t>(p.pq[1]) << 32 : 0ull);
-        const uint64_t half = p.phalf[0] | (lp > 1 ? static_cast<uint64_t>(p.phalf[1]) << 32 : 0ull);
-        uint64_t v = t[lp] | (lp > 1 ? static_cast<uint64_t>(t[lp + 1]) << 32 : 0ull);
-        if (t[2 * lp] || v >= q)
+        else
         {
-            v -= q;
+            const uint64_t t = (static_cast<uint64_t>(m[0] * p.pninv) * p.pq[0] + m[0]) >> 32;  // <= q
+            v = t >= q ? t - q : t;
         }
         return v > half ? static_cast<long long>(v) - static_cast<long long>(q) : static_cast<long long>(v);
     }
