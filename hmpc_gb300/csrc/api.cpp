@@ -442,6 +442,19 @@ int hmpc_context_destroy(hmpc_context* ctx)
     cudaFree(ctx->workspace);
     cudaFree(ctx->tc_workspace);
     cudaFree(ctx->tc_error);
+    if (ctx->aux_stream)
+    {
+        cudaStreamSynchronize(ctx->aux_stream);
+        cudaStreamDestroy(ctx->aux_stream);
+    }
+    if (ctx->fork_event)
+    {
+        cudaEventDestroy(ctx->fork_event);
+    }
+    if (ctx->join_event)
+    {
+        cudaEventDestroy(ctx->join_event);
+    }
     delete ctx;
     return HMPC_OK;
 }
@@ -1243,13 +1256,41 @@ int hmpc_lhe_keygen(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_
         return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating the key workspace");
     }
     int rc = hmpc_sample_uniform(ctx, q, n, 80, b);
+    // s and e are independent transforms; on the CUDA-core passes (no shared
+    // workspace) e's runs on the context's second stream meanwhile.  The
+    // nonces are taken on the host in the reference's order either way.
+    bool fork = false;
+    if (!rc)
+    {
+        std::lock_guard<std::mutex> lock(q->tables_mutex);
+        auto it = q->tile_choices.find(std::make_tuple(__builtin_ctzll(n), 0, static_cast<uint64_t>(1)));
+        const int radix = it == q->tile_choices.end() ? hmpc_modulus::TileChoice{}.radix_bits : it->second.radix_bits;
+        fork = radix != 0 && __builtin_ctzll(n) >= q->kt->radix_bits;
+    }
+    fork = fork && ctx->aux();
+    if (fork)
+    {
+        HMPC_CUDA(cudaEventRecord(ctx->fork_event, ctx->stream), "forking the key generation");
+        HMPC_CUDA(cudaStreamWaitEvent(ctx->aux_stream, ctx->fork_event, 0), "forking the key generation");
+    }
     if (!rc)
     {
         rc = run_transform(ctx, q, n, 1, false, producer_cbd, 1, 0, nullptr, s);
     }
     if (!rc)
     {
+        cudaStream_t main = ctx->stream;
+        if (fork)
+        {
+            ctx->stream = ctx->aux_stream;
+        }
         rc = run_transform(ctx, q, n, 1, false, producer_cbd, 20, 0, nullptr, e_poly);
+        ctx->stream = main;
+    }
+    if (fork)
+    {
+        HMPC_CUDA(cudaEventRecord(ctx->join_event, ctx->aux_stream), "joining the key generation");
+        HMPC_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join_event, 0), "joining the key generation");
     }
     if (!rc)
     {

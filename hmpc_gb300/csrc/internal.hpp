@@ -92,6 +92,22 @@ struct hmpc_context
     uint64_t tc_workspace_words = 0;
     uint32_t* tc_error = nullptr;
     int sm_count = 0;
+    // a second stream for independent work of one call (fork / join events)
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t fork_event = nullptr;
+    cudaEvent_t join_event = nullptr;
+
+    bool aux()
+    {
+        if (!aux_stream &&
+            (cudaStreamCreateWithFlags(&aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+             cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming) != cudaSuccess ||
+             cudaEventCreateWithFlags(&join_event, cudaEventDisableTiming) != cudaSuccess))
+        {
+            return false;
+        }
+        return true;
+    }
 
     uint32_t* tc_scratch(uint64_t words)
     {
