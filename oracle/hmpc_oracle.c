@@ -881,6 +881,186 @@ void orc_binary(const orc_modulus* m, int op, uint64_t elements, const uint32_t*
     }
 }
 
+/* expr/matrix_vector_product.hpp:88-140: output element (b, i, c) is the
+ * fold over k of matrix(b, i, k, c) * vector(b, k, c) with mod<Q>'s product
+ * and sum; the matrix index inserts k after (b, i), the vector index replaces
+ * i by k (:101-113).  A batch extent of one broadcasts (:7-23). */
+void orc_matvec(const orc_modulus* m, uint64_t batch, uint64_t rows, uint64_t cols, uint64_t coeffs,
+                const uint32_t* mat, uint64_t m_batch, const uint32_t* x, uint64_t x_batch, uint32_t* z,
+                int threads)
+{
+    int L = m->limbs;
+    uint64_t m_el = m_batch * rows * cols * coeffs;
+    uint64_t x_el = x_batch * cols * coeffs;
+    uint64_t z_el = batch * rows * coeffs;
+    set_threads(threads);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < (int64_t)z_el; ++e)
+    {
+        uint64_t c = (uint64_t)e % coeffs, t = (uint64_t)e / coeffs;
+        uint64_t i = t % rows, b = t / rows;
+        uint64_t bm = m_batch == 1 ? 0 : b, bx = x_batch == 1 ? 0 : b;
+        uint32_t acc[ORC_MAX_LIMBS] = {0}, a[ORC_MAX_LIMBS], v[ORC_MAX_LIMBS], p[ORC_MAX_LIMBS];
+        for (uint64_t k = 0; k < cols; ++k)
+        {
+            load_planar(mat, m_el, ((bm * rows + i) * cols + k) * coeffs + c, L, a);
+            load_planar(x, x_el, (bx * cols + k) * coeffs + c, L, v);
+            orc_mul(m, p, a, v);
+            orc_add(m, acc, acc, p);
+        }
+        store_planar(z, z_el, (uint64_t)e, L, acc);
+    }
+}
+
+/* expr/bit_monomial.hpp:28-104: coefficient c of X^d * x is x[(c - d) mod n],
+ * negated when c - d (as an unsigned 64-bit difference) has bit log2(n) set
+ * (one wrap past X^n = -1); no monomial contributes zero (:98-101). */
+void orc_matvec_monomial(const orc_modulus* m, uint64_t n, uint64_t batch, uint64_t rows, uint64_t cols,
+                         const int64_t* degrees, uint64_t d_batch, const uint32_t* x, uint64_t x_batch,
+                         uint32_t* z, int threads)
+{
+    int L = m->limbs;
+    int bits = __builtin_ctzll(n);
+    uint64_t x_el = x_batch * cols * n;
+    uint64_t z_el = batch * rows * n;
+    set_threads(threads);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < (int64_t)z_el; ++e)
+    {
+        uint64_t c = (uint64_t)e % n, t = (uint64_t)e / n;
+        uint64_t i = t % rows, b = t / rows;
+        uint64_t bd = d_batch == 1 ? 0 : b, bx = x_batch == 1 ? 0 : b;
+        uint32_t acc[ORC_MAX_LIMBS] = {0}, v[ORC_MAX_LIMBS];
+        for (uint64_t k = 0; k < cols; ++k)
+        {
+            int64_t d = degrees[(bd * rows + i) * cols + k];
+            if (d < 0)
+            {
+                continue;
+            }
+            uint64_t difference = c - (uint64_t)d;
+            uint64_t src = difference & (n - 1);
+            int negative = (int)((difference >> bits) & 1u);
+            load_planar(x, x_el, (bx * cols + k) * n + src, L, v);
+            if (negative)
+            {
+                orc_neg(m, v, v);
+            }
+            orc_add(m, acc, acc, v);
+        }
+        store_planar(z, z_el, (uint64_t)e, L, acc);
+    }
+}
+
+/* expr/reduce.hpp:206-250 over mod<Q>: sycl::plus / sycl::multiplies on
+ * mod's operators, identities integer_traits<mod>::zero and ::one (the
+ * Montgomery form of 1, R mod Q; ints/integer_traits.hpp:75-76). */
+int orc_reduce_mod(const orc_modulus* m, int op, uint64_t elements, const uint32_t* in, uint32_t* out)
+{
+    int L = m->limbs;
+    uint32_t acc[ORC_MAX_LIMBS] = {0}, v[ORC_MAX_LIMBS];
+    if (op == ORC_REDUCE_MULTIPLY)
+    {
+        memcpy(acc, m->one, sizeof(uint32_t) * (size_t)L);
+    }
+    else if (op != ORC_REDUCE_ADD)
+    {
+        return 1;
+    }
+    for (uint64_t e = 0; e < elements; ++e)
+    {
+        load_planar(in, elements, e, L, v);
+        if (op == ORC_REDUCE_ADD)
+        {
+            orc_add(m, acc, acc, v);
+        }
+        else
+        {
+            orc_mul(m, acc, acc, v);
+        }
+    }
+    memcpy(out, acc, sizeof(uint32_t) * (size_t)L);
+    return 0;
+}
+
+static void mask_bits(uint32_t* x, int limbs, int bits)
+{
+    if (bits % 32)
+    {
+        x[limbs - 1] &= (1u << (bits % 32)) - 1u;
+    }
+}
+
+/* expr/reduce.hpp:206-250 over uint<bits> (ints/uint.hpp): identities of
+ * ints/integer_traits.hpp:39-46 (zero, one, all_ones = compl all_zeros,
+ * max = all_ones, min = zero); the accumulator is a uint<bits>, so sums and
+ * products keep their low `bits` bits. */
+int orc_reduce_uint(int op, int bits, uint64_t elements, const uint32_t* in, uint32_t* out)
+{
+    if (bits < 1 || bits > 32 * ORC_MAX_LIMBS / 2 || op < ORC_REDUCE_ADD || op > ORC_REDUCE_MAX)
+    {
+        return 1;
+    }
+    int L = (bits + 31) / 32;
+    uint32_t acc[ORC_MAX_LIMBS] = {0}, v[ORC_MAX_LIMBS], wide[2 * ORC_MAX_LIMBS];
+    if (op == ORC_REDUCE_MULTIPLY)
+    {
+        acc[0] = 1;
+    }
+    else if (op == ORC_REDUCE_BIT_AND || op == ORC_REDUCE_MIN)
+    {
+        memset(acc, 0xff, sizeof(uint32_t) * (size_t)L);
+        mask_bits(acc, L, bits);
+    }
+    for (uint64_t e = 0; e < elements; ++e)
+    {
+        load_planar(in, elements, e, L, v);
+        mask_bits(v, L, bits);
+        switch (op)
+        {
+        case ORC_REDUCE_ADD:
+            big_add(acc, acc, v, L);
+            break;
+        case ORC_REDUCE_MULTIPLY:
+            big_mul(wide, acc, L, v, L);
+            memcpy(acc, wide, sizeof(uint32_t) * (size_t)L);
+            break;
+        case ORC_REDUCE_BIT_AND:
+            for (int j = 0; j < L; ++j) acc[j] &= v[j];
+            break;
+        case ORC_REDUCE_BIT_OR:
+            for (int j = 0; j < L; ++j) acc[j] |= v[j];
+            break;
+        case ORC_REDUCE_BIT_XOR:
+            for (int j = 0; j < L; ++j) acc[j] ^= v[j];
+            break;
+        case ORC_REDUCE_MIN:
+            if (big_cmp(v, acc, L) < 0) memcpy(acc, v, sizeof(uint32_t) * (size_t)L);
+            break;
+        default:
+            if (big_cmp(v, acc, L) > 0) memcpy(acc, v, sizeof(uint32_t) * (size_t)L);
+            break;
+        }
+        mask_bits(acc, L, bits);
+    }
+    memcpy(out, acc, sizeof(uint32_t) * (size_t)L);
+    return 0;
+}
+
+/* binary_expression.hpp with operator== (core/equal_to.hpp): one hmpc::bit per element */
+void orc_equal(int limbs, uint64_t elements, const uint32_t* a, const uint32_t* b, uint32_t* out)
+{
+    for (uint64_t e = 0; e < elements; ++e)
+    {
+        uint32_t eq = 1;
+        for (int j = 0; j < limbs; ++j)
+        {
+            eq &= a[(uint64_t)j * elements + e] == b[(uint64_t)j * elements + e];
+        }
+        out[e] = eq;
+    }
+}
+
 /* expr/random/uniform.hpp:41-45 with the capability of comp/queue.hpp:191-212 */
 void orc_sample_uniform_tensor(const orc_modulus* m, uint64_t elements, const uint32_t key[8],
                                const uint32_t nonce[3], int security, uint32_t* out, int threads)

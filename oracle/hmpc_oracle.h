@@ -142,6 +142,40 @@ void orc_cast_tensor(const orc_modulus* dst, const orc_modulus* src, uint64_t el
 void orc_to_uint_tensor(const orc_modulus* m, uint64_t elements, const uint32_t* x, uint32_t* out, int threads);
 void orc_from_uint_tensor(const orc_modulus* m, uint64_t elements, const uint32_t* x, uint32_t* out, int threads);
 
+/* Matrix-vector product (expr/matrix_vector_product.hpp:88-140) of mod<Q>
+ * tensors: z[b][i][c] = sum_k m[b][i][k][c] * x[b][k][c], c < coeffs (the
+ * coefficients of NTT-form polynomials, whose ring product is elementwise).
+ * m_batch and x_batch are batch or 1 (a batch of one is broadcast, the
+ * common_extent of matrix_vector_product.hpp:7-23). */
+void orc_matvec(const orc_modulus* m, uint64_t batch, uint64_t rows, uint64_t cols, uint64_t coeffs,
+                const uint32_t* mat, uint64_t m_batch, const uint32_t* x, uint64_t x_batch, uint32_t* z,
+                int threads);
+/* The same product with a matrix of bit monomials X^d (expr/bit_monomial.hpp:
+ * 18-104) times polynomials of degree n in coefficient form mod Q:
+ * degrees[b][i][k] < 0 stands for std::nullopt (no monomial). */
+void orc_matvec_monomial(const orc_modulus* m, uint64_t n, uint64_t batch, uint64_t rows, uint64_t cols,
+                         const int64_t* degrees, uint64_t d_batch, const uint32_t* x, uint64_t x_batch,
+                         uint32_t* z, int threads);
+
+enum
+{
+    ORC_REDUCE_ADD = 0,
+    ORC_REDUCE_MULTIPLY = 1,
+    ORC_REDUCE_BIT_AND = 2,
+    ORC_REDUCE_BIT_OR = 3,
+    ORC_REDUCE_BIT_XOR = 4,
+    ORC_REDUCE_MIN = 5,
+    ORC_REDUCE_MAX = 6,
+};
+/* Reduction of every element to one value (expr/reduce.hpp:206-250).
+ * mod<Q>: add or multiply (returns 1 for other operations); out has L words. */
+int orc_reduce_mod(const orc_modulus* m, int op, uint64_t elements, const uint32_t* in, uint32_t* out);
+/* uint<bits> in ceil(bits/32) limb planes: every operation; sums and products
+ * wrap modulo 2^bits.  Returns 1 for a bad operation or width. */
+int orc_reduce_uint(int op, int bits, uint64_t elements, const uint32_t* in, uint32_t* out);
+/* out[e] = 1 if a[e] == b[e] (every limb) else 0: the hmpc::bit of x == y */
+void orc_equal(int limbs, uint64_t elements, const uint32_t* a, const uint32_t* b, uint32_t* out);
+
 /* Linear BGV (expr/crypto/lhe/enc.hpp:19-69): given key (a, b) in NTT form
  * mod q (one polynomial each) and `batch` plaintexts mod p, compute the
  * ciphertexts with the reference's execution order

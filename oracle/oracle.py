@@ -99,6 +99,17 @@ def lib():
                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
         _lib.orc_lhe_keygen.argtypes = [mp, mp, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        _lib.orc_matvec.argtypes = [mp] + [ctypes.c_uint64] * 4 + [ctypes.c_void_p, ctypes.c_uint64,
+                                                                    ctypes.c_void_p, ctypes.c_uint64,
+                                                                    ctypes.c_void_p, ctypes.c_int]
+        _lib.orc_matvec_monomial.argtypes = [mp] + [ctypes.c_uint64] * 4 + [ctypes.c_void_p, ctypes.c_uint64,
+                                                                             ctypes.c_void_p, ctypes.c_uint64,
+                                                                             ctypes.c_void_p, ctypes.c_int]
+        _lib.orc_reduce_mod.argtypes = [mp, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+        _lib.orc_reduce_uint.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p,
+                                         ctypes.c_void_p]
+        _lib.orc_equal.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p]
     return _lib
 
 
@@ -375,6 +386,58 @@ def cipher_dec(key, nonce, flat, limbs):
     elements = flat.size // limbs
     out = np.zeros((limbs, elements), dtype=np.uint32)
     lib().orc_cipher_dec(_u32(key), _u32(nonce), ctypes.c_uint64(elements), limbs, _ptr(flat), _ptr(out))
+    return out
+
+
+REDUCE_OPS = {"add": 0, "multiply": 1, "bit_and": 2, "bit_or": 3, "bit_xor": 4, "min": 5, "max": 6}
+
+
+def matvec(m, batch, rows, cols, coeffs, mat, x, threads=0):
+    """z[b][i][c] = sum_k mat[b][i][k][c] * x[b][k][c] mod Q; mat and x are
+    limb-planar with a batch of `batch` or 1 (broadcast)."""
+    mat = np.ascontiguousarray(mat, dtype=np.uint32)
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    m_batch = mat.shape[1] // (rows * cols * coeffs)
+    x_batch = x.shape[1] // (cols * coeffs)
+    z = np.zeros((m.limbs, batch * rows * coeffs), dtype=np.uint32)
+    lib().orc_matvec(m.ref, batch, rows, cols, coeffs, _ptr(mat), m_batch, _ptr(x), x_batch, _ptr(z), threads)
+    return z
+
+
+def matvec_monomial(m, n, batch, rows, cols, degrees, x, threads=0):
+    """z[b][i] = sum_k X^degrees[b][i][k] * x[b][k] in Z_Q[X]/(X^n + 1),
+    coefficient form; a negative degree is no monomial."""
+    degrees = np.ascontiguousarray(degrees, dtype=np.int64).reshape(-1)
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    d_batch = degrees.size // (rows * cols)
+    x_batch = x.shape[1] // (cols * n)
+    z = np.zeros((m.limbs, batch * rows * n), dtype=np.uint32)
+    lib().orc_matvec_monomial(m.ref, n, batch, rows, cols, _ptr(degrees), d_batch, _ptr(x), x_batch, _ptr(z),
+                              threads)
+    return z
+
+
+def reduce_mod(m, op, x):
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    out = np.zeros(m.limbs, dtype=np.uint32)
+    if lib().orc_reduce_mod(m.ref, REDUCE_OPS.get(op, op), x.shape[1], _ptr(x), _ptr(out)):
+        raise ValueError(f"bad reduction {op}")
+    return out
+
+
+def reduce_uint(op, bits, x):
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    out = np.zeros((bits + 31) // 32, dtype=np.uint32)
+    if lib().orc_reduce_uint(REDUCE_OPS.get(op, op), bits, x.shape[1], _ptr(x), _ptr(out)):
+        raise ValueError(f"bad reduction {op} over {bits} bits")
+    return out
+
+
+def equal(a, b):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    b = np.ascontiguousarray(b, dtype=np.uint32)
+    out = np.zeros(a.shape[1], dtype=np.uint32)
+    lib().orc_equal(a.shape[0], a.shape[1], _ptr(a), _ptr(b), _ptr(out))
     return out
 
 

@@ -182,6 +182,92 @@ def lhe_vectors(root):
     }
 
 
+def matvec_vectors(root):
+    """tests/expr/matrix_vector_product.cpp: a matrix of bit monomials (an
+    index tensor, std::nullopt for no monomial) times polynomials of degree
+    N with small integer coefficients, and the signed products it CHECKs."""
+    rel = "tests/expr/matrix_vector_product.cpp"
+    src = lines_of(root / rel)
+    text = "\n".join(src)
+    log_n = int(re.search(r"constexpr hmpc::size N = 1 << (\d+);", text).group(1))
+    rows = int(re.search(r"constexpr hmpc::size V = (\d+);", text).group(1))
+    cols = {"four": 4, "two": 2, "eight": 8}[re.search(r"constexpr auto U = hmpc::constants::(\w+);", text).group(1)]
+    index_shape = [int(x) if x.isdigit() else {"V": rows, "U": cols}[x]
+                   for x in re.search(r"index_shape = hmpc::shape\{(\w+), (\w+), (\w+)\};", text).groups()]
+    degrees, x, z = {}, {}, {}
+    first = last = None
+    for no, line in enumerate(src, 1):
+        m = re.search(r"indices\[hmpc::index\{(\d+), (\d+), (\d+)\}\] = (\d+|std::nullopt);", line)
+        if m:
+            key = tuple(int(v) for v in m.groups()[:3])
+            degrees[key] = -1 if m.group(4) == "std::nullopt" else int(m.group(4))
+            first = first or no
+        m = re.search(r"\bx\[hmpc::index\{(\d+), (\d+), (\d+)\}\] = uint\{(\d+)\};", line)
+        if m:
+            x[tuple(int(v) for v in m.groups()[:3])] = int(m.group(4))
+        m = re.search(r"CHECK\(z\[hmpc::index\{(\d+), (\d+), (\d+)\}\] == (-?)integer\{(\d+)\}\);", line)
+        if m:
+            value = int(m.group(5))
+            z[tuple(int(v) for v in m.groups()[:3])] = -value if m.group(4) else value
+            last = no
+    batch = index_shape[0]
+    n = 1 << log_n
+    return {
+        "file": rel,
+        "lines": f"{rel}:{first}-{last}",
+        "n": n,
+        "batch": batch,
+        "rows": rows,
+        "cols": cols,
+        # degrees[b][i][k], -1 = std::nullopt
+        "degrees": [[[degrees[(b, i, k)] for k in range(cols)] for i in range(rows)] for b in range(batch)],
+        # x[b][k][c] and z[b][i][c]
+        "x": [[[x[(b, k, c)] for c in range(n)] for k in range(cols)] for b in range(batch)],
+        "z": [[[z[(b, i, c)] for c in range(n)] for i in range(rows)] for b in range(batch)],
+    }
+
+
+def reduce_vectors(root):
+    """tests/expr/reduce.cpp: x_i = 3i + 1 and y_i = i + 1 as uint<127>, the
+    reductions of x and the all/any of x == y that it CHECKs."""
+    rel = "tests/expr/reduce.cpp"
+    src = lines_of(root / rel)
+    text = "\n".join(src)
+    count = int(re.search(r"constexpr auto N = (\d+);", text).group(1))
+    bits = int(re.search(r"using uint = hmpc::ints::uint<(\d+)>;", text).group(1))
+    ax, bx = (int(v) for v in re.search(r"access_x\[i\] = uint\{static_cast<limb>\((\d+) \* i \+ (\d+)\)\};",
+                                         text).groups())
+    ay = re.search(r"access_y\[i\] = uint\{static_cast<limb>\(i \+ (\d+)\)\};", text)
+    checks = {}
+    names = {"sum": "add", "product": "multiply", "bit_or": "bit_or", "bit_and": "bit_and", "bit_xor": "bit_xor",
+             "min": "min", "max": "max"}
+    current = None
+    for no, line in enumerate(src, 1):
+        m = re.search(r"host_accessor (\w+)\((\w+)_tensor, hmpc::access::read\);", line)
+        if m:
+            current = m.group(1)
+        m = re.search(r"CHECK\(value == uint\{(\d+)\}\);", line)
+        if m and current in names:
+            checks[names[current]] = {"value": int(m.group(1)), "line": f"{rel}:{no}"}
+        m = re.search(r"size_limb_span<limb>\(([\d']+)\)\)\);", line)
+        if m and current in names:
+            checks[names[current]] = {"value": int(m.group(1).replace("'", "")), "line": f"{rel}:{no}"}
+        m = re.search(r"CHECK(_FALSE)?\(value( == hmpc::bit\{true\})?\);", line)
+        if m and current in ("all", "any"):
+            key = {"all": "all_x_eq_y", "any": "any_x_eq_y"}[current]
+            if current == "all" and "all_equal_tensor" in "\n".join(src[max(0, no - 4):no]):
+                key = "all_x_eq_x"
+            checks.setdefault(key, {"value": m.group(1) is None, "line": f"{rel}:{no}"})
+    return {
+        "file": rel,
+        "count": count,
+        "bits": bits,
+        "x": [ax * i + bx for i in range(count)],
+        "y": [i + int(ay.group(1)) for i in range(count)],
+        "checks": checks,
+    }
+
+
 def main():
     root = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     data = {
@@ -192,6 +278,8 @@ def main():
         "poly_mod_ntt": poly_mod_vectors(root),
         "root_of_unity": root_of_unity_vectors(root),
         "linear_bgv": lhe_vectors(root),
+        "matrix_vector_product": matvec_vectors(root),
+        "reduce": reduce_vectors(root),
     }
     out = pathlib.Path(__file__).with_name("reference_kats.json")
     out.write_text(json.dumps(data, indent=1, default=str) + "\n")
