@@ -48,8 +48,7 @@ CONFIG = {
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
 # kernel: mean over the five tc_group_kernel launches of one fused CBD(10)
-# transform of 256 x 2^15 (one-pass metrics captured at this size;
-# profiles/tc_group_kernel_cbd_n32768_L8_traffic.md)
+# transform of 256 x 2^15 (one-pass ncu metrics captured at this size)
 DOMINANT_TRAFFIC_BYTES = 711.9e6
 
 
@@ -282,6 +281,7 @@ def secondary_metrics(queue, int_peak):
     network messages (HBM-bound copy)."""
     import torch
 
+    from hmpc_gb300 import _lib
     from hmpc_gb300.batch import NttBatch, uneven_degrees
     from hmpc_gb300.comp import Tensor
     from hmpc_gb300.workloads import MODULI
@@ -309,7 +309,29 @@ def secondary_metrics(queue, int_peak):
     ms = time_ms(lambda: queue.fma(a, b, c, out=d), 20)
     gbs = count * 64 / (ms * 1e-3) / 1e9
     out["fma_2^24_L4"] = {"ms": ms, "GB/s": gbs, "hbm_frac": gbs / peak, "hbm_peak_source": source}
-    del a, b, c, d
+
+    # sum of the same 2^24 residues: one read of 16 B each (two launches)
+    total = Tensor(qf, ())
+    ms = time_ms(lambda: _lib.call("hmpc_reduce", queue.handle, qf.handle, 0, count, a.ptr(), total.ptr()), 20)
+    gbs = count * 16 / (ms * 1e-3) / 1e9
+    out["sum_2^24_L4"] = {"ms": ms, "GB/s": gbs, "hbm_frac": gbs / peak, "hbm_peak_source": source}
+    del a, b, c, d, total
+
+    # matrix-vector product of NTT-form polynomials: 16 x (4 x 4 matrix) times
+    # 4-vectors of degree 2^15, q 256-bit (8 limbs): one Montgomery product per
+    # matrix coefficient, so bound by the integer multiply rate
+    qm = queue.modulus(Q_256)
+    mb, rows, cols = 16, 4, 4
+    mm = queue.uniform(qm, (mb, rows, cols), N)
+    xv = queue.uniform(qm, (mb, cols), N)
+    zv = Tensor(qm, (mb, rows), N)
+    ms = time_ms(lambda: queue.matrix_vector_product(mm, xv, out=zv), 20)
+    products = mb * rows * cols * N
+    moved = (mm.elements + xv.elements + zv.elements) * 8 * 4
+    out["matvec_16x4x4_n32768_L8"] = {"ms": ms, "GB/s": moved / (ms * 1e-3) / 1e9,
+                                      "int_frac": products * mont_mul_ops(8) / (ms * 1e-3) / int_peak,
+                                      "hbm_frac": moved / (ms * 1e-3) / 1e9 / peak}
+    del mm, xv, zv
 
     # single transform N = 4096, q 125-bit (examples/ntt.cpp modulus), batch 1:
     # NTT then INTT, replayed from a CUDA graph so the device time is measured

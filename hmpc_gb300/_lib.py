@@ -23,6 +23,7 @@ PRODUCER_TENSOR = 0
 PRODUCER_CBD = 1
 PRODUCER_UNIFORM = 2
 OP_ADD, OP_SUB, OP_MUL = 0, 1, 2
+REDUCE_OPS = {"add": 0, "multiply": 1, "bit_and": 2, "bit_or": 3, "bit_xor": 4, "min": 5, "max": 6}
 
 
 class HmpcError(RuntimeError):
@@ -123,6 +124,11 @@ SIGNATURES = {
     "hmpc_lhe_enc_noalloc": ([_vp, _vp, _vp, _u64, _u64, _vp, _vp, _vp, _int, _vp, _vp], _int),
     "hmpc_lhe_dec": ([_vp, _vp, _vp, _u64, _u64, _vp, _vp, _vp, _int, _vp], _int),
     "hmpc_lhe_keygen": ([_vp, _vp, _vp, _u64, _vp, _vp, _vp], _int),
+    "hmpc_matvec": ([_vp, _vp, _u64, _u64, _u64, _u64, _vp, _u64, _vp, _u64, _vp], _int),
+    "hmpc_matvec_monomial": ([_vp, _vp, _u64, _u64, _u64, _u64, _vp, _u64, _vp, _u64, _vp], _int),
+    "hmpc_reduce": ([_vp, _vp, _int, _u64, _vp, _vp], _int),
+    "hmpc_reduce_uint": ([_vp, _int, _int, _u64, _vp, _vp], _int),
+    "hmpc_equal": ([_vp, _int, _u64, _vp, _vp, _vp], _int),
 }
 
 _lib = None

@@ -62,7 +62,7 @@ def build(verbose=False, jobs=None):
         if _stale(obj, [CSRC / "tensor_ntt.cu", *headers]):
             steps.append(common + [f"-DHMPC_L={limbs}", "-c", str(CSRC / "tensor_ntt.cu"), "-o", str(obj)])
     for name in ("api.cpp", "host_math.cpp", "probe.cu", "noalloc.cu", "batched.cpp", "serve.cpp", "cipher.cu",
-                 "tc.cpp", "wire.cu"):
+                 "tc.cpp", "wire.cu", "linalg.cpp"):
         obj = OUT / (name.rsplit(".", 1)[0] + ".o")
         objects.append(obj)
         if _stale(obj, [CSRC / name, *headers]):

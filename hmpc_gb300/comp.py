@@ -300,3 +300,75 @@ class Queue:
         out = out or make_tensor(x.modulus, x.shape, x.n)
         _lib.call("hmpc_from_montgomery", self.handle, x.modulus.handle, x.elements, x.ptr(), out.ptr())
         return out
+
+    # ------------------------------------------- matrix products, reductions
+    def matrix_vector_product(self, m, x, out=None):
+        """hmpc::expr::matrix_vector_product(m, x) of residue tensors
+        (hmpc/expr/matrix_vector_product.hpp:88-140): m has shape
+        (batch or 1, rows, cols), x shape (batch or 1, cols), both with the
+        same n (coefficients of NTT-form polynomials, whose ring product is
+        elementwise; 1 for plain residues); the result has shape (batch, rows)."""
+        mb, rows, cols = m.shape
+        xb, xcols = x.shape
+        if xcols != cols or m.n != x.n:
+            raise ValueError("matrix columns and vector length differ")
+        batch = max(mb, xb)
+        out = out or make_tensor(m.modulus, (batch, rows), m.n)
+        _lib.call("hmpc_matvec", self.handle, m.modulus.handle, batch, rows, cols, m.n, m.ptr(), mb, x.ptr(), xb,
+                  out.ptr())
+        return out
+
+    def monomial_matrix_vector_product(self, degrees, x, out=None):
+        """matrix_vector_product(bit_monomial<n>(degrees), x)
+        (hmpc/expr/bit_monomial.hpp:18-165): degrees is an int64 device
+        tensor of shape (batch or 1, rows, cols), -1 for std::nullopt; x holds
+        coefficient-form polynomials of shape (batch or 1, cols)."""
+        db, rows, cols = degrees.shape
+        xb, xcols = x.shape
+        if xcols != cols or degrees.dtype != torch.int64 or not degrees.is_contiguous():
+            raise ValueError("degrees must be a contiguous int64 tensor matching the vector length")
+        batch = max(db, xb)
+        out = out or make_tensor(x.modulus, (batch, rows), x.n)
+        _lib.call("hmpc_matvec_monomial", self.handle, x.modulus.handle, x.n, batch, rows, cols, _ptr(degrees), db,
+                  x.ptr(), xb, out.ptr())
+        return out
+
+    def reduce(self, x, op):
+        """hmpc::expr::reduce(x, op) of a residue tensor to one value
+        (hmpc/expr/reduce.hpp:206-277): op "add" or "multiply"."""
+        out = make_tensor(x.modulus, ())
+        _lib.call("hmpc_reduce", self.handle, x.modulus.handle, _lib.REDUCE_OPS[op], x.elements, x.ptr(), out.ptr())
+        return out
+
+    def sum(self, x):
+        return self.reduce(x, "add")
+
+    def product(self, x):
+        return self.reduce(x, "multiply")
+
+    def reduce_uint(self, data, bits, op):
+        """reduce over uint<bits> values held limb-planar in an int32 device
+        tensor of shape (ceil(bits / 32), elements); returns the (limbs,) value"""
+        limbs = (bits + 31) // 32
+        if data.dim() != 2 or data.shape[0] != limbs or data.dtype != torch.int32 or not data.is_contiguous():
+            raise ValueError("uint tensors are contiguous int32 [limbs][elements]")
+        out = torch.empty(limbs, dtype=torch.int32, device=self.device)
+        _lib.call("hmpc_reduce_uint", self.handle, _lib.REDUCE_OPS[op], bits, data.shape[1], _ptr(data), _ptr(out))
+        return out
+
+    def equal(self, a, b):
+        """the hmpc::bit tensor of a == b (one int32 0/1 per element) for two
+        limb-planar int32 tensors of the same shape"""
+        if a.shape != b.shape or a.dim() != 2:
+            raise ValueError("operands differ in shape")
+        out = torch.empty(a.shape[1], dtype=torch.int32, device=self.device)
+        _lib.call("hmpc_equal", self.handle, a.shape[0], a.shape[1], _ptr(a), _ptr(b), _ptr(out))
+        return out
+
+    def all(self, bits):
+        """hmpc::expr::all of a bit tensor (one int32 0/1 per element)"""
+        return bool(self.reduce_uint(bits.reshape(1, -1), 1, "bit_and").item())
+
+    def any(self, bits):
+        """hmpc::expr::any of a bit tensor"""
+        return bool(self.reduce_uint(bits.reshape(1, -1), 1, "bit_or").item())

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "chacha.cuh"
+#include "linalg.cuh"
 #include "ntt.cuh"
 #include "plain.cuh"
 #include "tensor_ntt.cuh"
@@ -80,6 +81,16 @@ namespace hmpc_gb300
         cudaError_t (*lhe_combine_pair)(uint32_t* c0, uint32_t* c1, const uint32_t* ka, const uint32_t* kb,
                                         uint64_t n, const uint32_t* stacked, uint64_t elements,
                                         const HostModulus& m, cudaStream_t stream);
+        // matrix-vector products (linalg.cuh)
+        cudaError_t (*matvec)(uint32_t* z, const uint32_t* mat, const uint32_t* x, const MatvecParams& p,
+                              const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*matvec_monomial)(uint32_t* z, const int64_t* degrees, const uint32_t* x,
+                                       const MatvecParams& p, const HostModulus& m, cudaStream_t stream);
+        // one level of a reduction into `grid` values (mod: mod<Q> with m, else uint with top_mask)
+        cudaError_t (*reduce)(uint32_t* out, const uint32_t* in, uint64_t elements, int op, bool mod,
+                              uint32_t top_mask, unsigned grid, const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*equal)(uint32_t* out, const uint32_t* a, const uint32_t* b, uint64_t elements,
+                             cudaStream_t stream);
     };
 
     // sizes of one tensor-core group kernel instantiation (TcShape)

@@ -5,6 +5,7 @@
 #include "cast.cuh"
 #include "dispatch.hpp"
 #include "elementwise.cuh"
+#include "linalg.cuh"
 #include "ntt.cuh"
 
 #ifndef HMPC_L
@@ -363,9 +364,61 @@ namespace hmpc_gb300
             return cudaGetLastError();
         }
 
+        cudaError_t matvec(uint32_t* z, const uint32_t* mat, const uint32_t* x, const MatvecParams& p,
+                           const HostModulus& h, cudaStream_t stream)
+        {
+            if (p.total == 0)
+            {
+                return cudaSuccess;
+            }
+            matvec_kernel<L><<<grid_for(p.total, 256), 256, 0, stream>>>(z, mat, x, p, device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t matvec_monomial(uint32_t* z, const int64_t* degrees, const uint32_t* x, const MatvecParams& p,
+                                    const HostModulus& h, cudaStream_t stream)
+        {
+            if (p.total == 0)
+            {
+                return cudaSuccess;
+            }
+            matvec_monomial_kernel<L><<<grid_for(p.total, 256), 256, 0, stream>>>(z, degrees, x, p,
+                                                                                device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t reduce(uint32_t* out, const uint32_t* in, uint64_t elements, int op, bool mod,
+                           uint32_t top_mask, unsigned grid, const HostModulus& h, cudaStream_t stream)
+        {
+            const bool vectorised = elements % vec == 0 && reinterpret_cast<uintptr_t>(in) % 16 == 0;
+            if (mod)
+            {
+                const Reducer<L, true> red{op, 0xffffffffu, device_modulus(h)};
+                reduce_kernel<L, true><<<grid, 256, 0, stream>>>(out, grid, in, elements, vectorised, red);
+            }
+            else
+            {
+                const Reducer<L, false> red{op, top_mask, Modulus<L>{}};
+                reduce_kernel<L, false><<<grid, 256, 0, stream>>>(out, grid, in, elements, vectorised, red);
+            }
+            return cudaGetLastError();
+        }
+
+        cudaError_t equal(uint32_t* out, const uint32_t* a, const uint32_t* b, uint64_t elements,
+                          cudaStream_t stream)
+        {
+            if (elements == 0)
+            {
+                return cudaSuccess;
+            }
+            equal_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(out, a, b, elements);
+            return cudaGetLastError();
+        }
+
         const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd, to_montgomery,
                                    from_montgomery, cast, plain_stage, ct_mul, dec_combine, ntt_batched,
-                                   ntt_batched_blocks_per_sm, R, lhe_combine_pair};
+                                   ntt_batched_blocks_per_sm, R, lhe_combine_pair, matvec, matvec_monomial,
+                                   reduce, equal};
     }
 
     const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()

@@ -219,6 +219,51 @@ int hmpc_cast(hmpc_context* ctx, hmpc_modulus* dst, hmpc_modulus* src, uint64_t 
 int hmpc_to_montgomery(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* in, uint32_t* out);
 int hmpc_from_montgomery(hmpc_context* ctx, hmpc_modulus* mod, uint64_t elements, const uint32_t* in, uint32_t* out);
 
+/* --- matrix-vector products and reductions ------------------------------------
+ * The consumers of NTT-form data after the transform.  All tensors are
+ * limb-planar and row-major. */
+/* z[b][i][c] = sum_k m[b][i][k][c] * x[b][k][c] mod Q for b < batch, i < rows,
+ * k < cols, c < coeffs: hmpc::expr::matrix_vector_product of mod<Q> tensors
+ * (hmpc/expr/matrix_vector_product.hpp:88-140).  coeffs is 1 for a matrix of
+ * residues, or the degree for NTT-form polynomials, whose ring product is
+ * elementwise.  m holds m_batch matrices of rows x cols x coeffs elements and
+ * x holds x_batch vectors of cols x coeffs elements; each of m_batch and
+ * x_batch is batch or 1 (broadcast: the common_extent of
+ * matrix_vector_product.hpp:7-23).  z holds batch x rows x coeffs elements. */
+int hmpc_matvec(hmpc_context* ctx, hmpc_modulus* mod, uint64_t batch, uint64_t rows, uint64_t cols, uint64_t coeffs,
+                const uint32_t* m, uint64_t m_batch, const uint32_t* x, uint64_t x_batch, uint32_t* z);
+/* z[b][i] = sum_k X^degrees[b][i][k] * x[b][k] in Z_Q[X]/(X^n + 1) for
+ * polynomials of degree n (a power of two) in coefficient form: a matrix of
+ * hmpc::expr::bit_monomial<n> times polynomials (hmpc/expr/bit_monomial.hpp:
+ * 18-104 inside matrix_vector_product.hpp:88-140).  degrees is a device array
+ * of d_batch x rows x cols int64 values; a negative degree stands for
+ * std::nullopt (no monomial); a degree d acts as X^(d mod 2n).  x holds
+ * x_batch x cols polynomials, z batch x rows polynomials. */
+int hmpc_matvec_monomial(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, uint64_t rows,
+                         uint64_t cols, const int64_t* degrees, uint64_t d_batch, const uint32_t* x,
+                         uint64_t x_batch, uint32_t* z);
+#define HMPC_REDUCE_ADD 0
+#define HMPC_REDUCE_MULTIPLY 1
+#define HMPC_REDUCE_BIT_AND 2
+#define HMPC_REDUCE_BIT_OR 3
+#define HMPC_REDUCE_BIT_XOR 4
+#define HMPC_REDUCE_MIN 5
+#define HMPC_REDUCE_MAX 6
+/* out (device, L words) = the sum or product of every residue of in:
+ * hmpc::expr::sum / product of a mod<Q> tensor (hmpc/expr/reduce.hpp:206-277);
+ * op is HMPC_REDUCE_ADD or HMPC_REDUCE_MULTIPLY.  An empty tensor gives the
+ * identity (0, or the Montgomery form of 1). */
+int hmpc_reduce(hmpc_context* ctx, hmpc_modulus* mod, int op, uint64_t elements, const uint32_t* in, uint32_t* out);
+/* The same over uint<bits> values in ceil(bits / 32) limb planes (bits <= 288):
+ * every HMPC_REDUCE_* operation of hmpc::reduction (reduce.hpp:8-53); sums and
+ * products keep their low `bits` bits, as a uint<bits> accumulator does, and
+ * the identities are ints/integer_traits.hpp:39-46.  On one-bit values
+ * BIT_AND and BIT_OR are hmpc::expr::all and any. */
+int hmpc_reduce_uint(hmpc_context* ctx, int op, int bits, uint64_t elements, const uint32_t* in, uint32_t* out);
+/* out[e] = 1 if a[e] == b[e] in every limb, else 0: the hmpc::bit tensor of
+ * x == y (hmpc/expr/binary_expression.hpp) that all / any reduce. */
+int hmpc_equal(hmpc_context* ctx, int limbs, uint64_t elements, const uint32_t* a, const uint32_t* b, uint32_t* out);
+
 /* --- linear BGV (hmpc/expr/crypto/lhe) ---------------------------------------
  * Keys and ciphertext components are polynomials of degree n mod q in NTT
  * representation; plaintexts are mod p (coefficient representation, or NTT

@@ -17,6 +17,7 @@
 // in the reference's order (comp/queue.hpp:241-253).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cstdint>
 #include <map>
@@ -178,6 +179,9 @@ namespace hmpc
             multiply,
             cast,
             lhe_combine,
+            matrix_vector_product,
+            sum,
+            product,
         };
 
         // A node of the lazy expression DAG.  Nodes are shared; identity
@@ -288,6 +292,46 @@ namespace hmpc
             e->n = a->n;
             e->children = {std::move(a), std::move(b)};
             return e;
+        }
+
+        // matrix_vector_product(m, x) (expr/matrix_vector_product.hpp:125-143):
+        // m of shape {batch or 1, rows, cols}, x of shape {batch or 1, cols},
+        // both of the same modulus and degree; the result has shape {batch, rows}
+        inline expression matrix_vector_product(expression m, expression x)
+        {
+            if (m->shape.size() != 3 || x->shape.size() != 2 || m->shape[2] != x->shape[1] || m->n != x->n ||
+                m->mod != x->mod)
+            {
+                throw error(HMPC_ERROR_INVALID_ARGUMENT,
+                            "matrix_vector_product takes shapes {batch, rows, cols} and {batch, cols}");
+            }
+            auto e = std::make_shared<node>();
+            e->k = kind::matrix_vector_product;
+            e->mod = m->mod;
+            e->shape = {std::max(m->shape[0], x->shape[0]), m->shape[1]};
+            e->n = m->n;
+            e->children = {std::move(m), std::move(x)};
+            return e;
+        }
+
+        // sum(e) / product(e) of every residue (expr/reduce.hpp:257-267): a
+        // rank-0 result
+        inline expression reduction(kind k, expression inner)
+        {
+            auto e = std::make_shared<node>();
+            e->k = k;
+            e->mod = inner->mod;
+            e->n = 1;
+            e->children = {std::move(inner)};
+            return e;
+        }
+        inline expression sum(expression e)
+        {
+            return reduction(kind::sum, std::move(e));
+        }
+        inline expression product(expression e)
+        {
+            return reduction(kind::product, std::move(e));
         }
 
         namespace operators
@@ -469,6 +513,20 @@ namespace hmpc
                                       b.elements(), out.data()));
                     break;
                 }
+                case expr::kind::matrix_vector_product:
+                {
+                    const auto& m = e->children[0];
+                    const auto& x = e->children[1];
+                    check(hmpc_matvec(ctx_, e->mod->handle(), e->shape[0], m->shape[1], m->shape[2], e->n,
+                                      child(0).data(), m->shape[0], child(1).data(), x->shape[0], out.data()));
+                    break;
+                }
+                case expr::kind::sum:
+                case expr::kind::product:
+                    check(hmpc_reduce(ctx_, e->mod->handle(),
+                                      e->k == expr::kind::sum ? HMPC_REDUCE_ADD : HMPC_REDUCE_MULTIPLY,
+                                      child(0).elements(), child(0).data(), out.data()));
+                    break;
                 default:
                     throw error(HMPC_ERROR_UNSUPPORTED, "expression node not supported by this front end");
                 }

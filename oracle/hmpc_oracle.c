@@ -997,7 +997,7 @@ static void mask_bits(uint32_t* x, int limbs, int bits)
  * products keep their low `bits` bits. */
 int orc_reduce_uint(int op, int bits, uint64_t elements, const uint32_t* in, uint32_t* out)
 {
-    if (bits < 1 || bits > 32 * ORC_MAX_LIMBS / 2 || op < ORC_REDUCE_ADD || op > ORC_REDUCE_MAX)
+    if (bits < 1 || bits > 32 * ORC_MAX_LIMBS || op < ORC_REDUCE_ADD || op > ORC_REDUCE_MAX)
     {
         return 1;
     }

@@ -59,6 +59,23 @@ int main(int argc, char** argv)
     auto w = queue(expr::inverse_number_theoretic_transform(expr::tensor(a) * expr::tensor(u) + expr::tensor(v)));
     dump(dir, "w.bin", w.download());
 
+    // a 2 x 3 matrix of NTT-form polynomials times the 3 polynomials of y
+    // (broadcast over a batch of one), and the sum and product of y
+    auto mat = hmpc::comp::make_tensor(queue, q, {1, 2, batch}, n);
+    std::vector<uint32_t> mhost(mat.words(), 0u);
+    for (uint64_t e = 0; e < 2 * batch * n; ++e)
+    {
+        mhost[e] = static_cast<uint32_t>(3 * e + 7);
+    }
+    mat.upload(mhost);
+    auto vec = hmpc::comp::make_tensor(queue, q, {1, batch}, n);
+    vec.upload(y.download());
+    auto [z, total, prod] = queue(expr::matrix_vector_product(expr::tensor(mat), expr::tensor(vec)),
+                                  expr::sum(expr::tensor(y)), expr::product(expr::tensor(y)));
+    dump(dir, "matvec.bin", z.download());
+    dump(dir, "sum.bin", total.download());
+    dump(dir, "product.bin", prod.download());
+
     // BGV round trip through the lhe front end
     auto [s, key] = hmpc::crypto::lhe::keygen(queue, q, p, n);
     auto m = queue(expr::uniform(p, {batch}, n));

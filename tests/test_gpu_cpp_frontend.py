@@ -40,3 +40,9 @@ def test_cpp_frontend(tmp_path, oracle):
     au = oracle.binary(m, oracle.OP_MUL, a, u, elements=n * batch)
     w = oracle.ntt(m, n, batch, src=oracle.binary(m, oracle.OP_ADD, au, v), inverse=True)
     assert np.array_equal(load("w.bin"), w)
+    y = load("ntt.bin")
+    mat = np.zeros((m.limbs, 2 * batch * n), dtype=np.uint32)
+    mat[0] = 3 * np.arange(2 * batch * n, dtype=np.uint32) + 7
+    assert np.array_equal(load("matvec.bin"), oracle.matvec(m, 1, 2, batch, n, mat, y))
+    assert np.array_equal(load("sum.bin")[:, 0], oracle.reduce_mod(m, "add", y))
+    assert np.array_equal(load("product.bin")[:, 0], oracle.reduce_mod(m, "multiply", y))

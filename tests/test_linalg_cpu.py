@@ -116,7 +116,7 @@ def test_reduce_mod_matches_python_integers(oracle, q):
         oracle.reduce_mod(m, "bit_or", x)
 
 
-@pytest.mark.parametrize("bits", [1, 31, 32, 127, 256])
+@pytest.mark.parametrize("bits", [1, 31, 32, 127, 256, 288])
 def test_reduce_uint_identities_and_wraparound(oracle, bits):
     rng = random.Random(bits)
     limbs = (bits + 31) // 32
