@@ -358,10 +358,13 @@ def secondary_metrics(queue, int_peak):
             queue.set_stream(stream)
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(side)
-            for _ in range(reps):
-                g.replay()
-            b.record(side)
+            # a graph replays on torch's current stream: make it the stream the
+            # events are recorded on, so they bracket the replays' device time
+            with torch.cuda.stream(side):
+                a.record(side)
+                for _ in range(reps):
+                    g.replay()
+                b.record(side)
             torch.cuda.synchronize()
             return a.elapsed_time(b) / reps
         finally:
@@ -450,6 +453,89 @@ def secondary_metrics(queue, int_peak):
                                           "bytes_read_plus_written": moved}
     del parts, buf
     return out
+
+
+def plain_encryption_comparison(queue, q, p, s, key, msgs, ct):
+    """The batch's encryption against the plain GPU path: one call chain per
+    ciphertext, every transform one launch per stage (the reference's
+    stage-per-kernel schedule): NTT(u), NTT(v), NTT(lift(m)), NTT(w) and the
+    elementwise combines c0 = a*u + p*v + m, c1 = b*u + p*w.  The plain
+    ciphertexts are decrypted to check that the path is a correct encryption
+    (its nonces are drawn per call, so its noise differs from the batch's)."""
+    import numpy as np
+    import torch
+
+    from hmpc_gb300 import lhe
+    from hmpc_gb300.comp import Tensor
+
+    stream = queue.stream
+    p_words = np.array([[P_64 & 0xFFFFFFFF] + [0] * (q.limbs - 1)], dtype=np.uint32).T.copy()
+    p_words[1, 0] = P_64 >> 32
+    p_mont = queue.to_montgomery(Tensor.from_numpy(q, p_words, (1,)))
+    parts = [Tensor(p, (1,), N, msgs.data[:, i * N:(i + 1) * N].contiguous()) for i in range(BATCH)]
+    outs = [lhe.Ciphertext(Tensor(q, (1,), N), Tensor(q, (1,), N)) for _ in range(BATCH)]
+    u, v, w, lift, mh, t = (Tensor(q, (1,), N) for _ in range(6))
+
+    def plain_one(m, out):
+        queue.ntt_plain_centered_binomial(q, N, (1,), 1, out=u)
+        queue.ntt_plain_centered_binomial(q, N, (1,), 20, out=v)
+        queue.cast(m, q, out=lift)
+        queue.ntt_plain(lift, out=mh)
+        queue.mul(key.a, u, out=out.c0)
+        queue.mul(p_mont, v, out=t)
+        queue.add(out.c0, t, out=out.c0)
+        queue.add(out.c0, mh, out=out.c0)
+        queue.ntt_plain_centered_binomial(q, N, (1,), 20, out=w)
+        queue.mul(key.b, u, out=out.c1)
+        queue.mul(p_mont, w, out=t)
+        queue.add(out.c1, t, out=out.c1)
+
+    def plain_all():
+        for m, out in zip(parts, outs):
+            plain_one(m, out)
+
+    def batched():
+        lhe.enc(queue, key, msgs, q, out=ct)
+
+    def time_ms(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    ms_plain = time_ms(plain_all, 2)
+    ms_batch = time_ms(batched, 10)
+    ok = all(bool((lhe.dec(queue, s, outs[i], p).data == parts[i].data).all().item()) for i in (0, BATCH - 1))
+    # the same launches replayed from one CUDA graph: the plain schedule's
+    # device time without the host's per-call overhead
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    queue.set_stream(side)
+    try:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side):
+            plain_all()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        # a graph replays on torch's current stream: the events' stream
+        with torch.cuda.stream(side):
+            graph.replay()
+            side.synchronize()
+            a.record(side)
+            graph.replay()
+            b.record(side)
+        side.synchronize()
+        ms_plain_graph = a.elapsed_time(b)
+    finally:
+        queue.set_stream(stream)
+    torch.cuda.synchronize()
+    return {"ms_batched": ms_batch, "ms_plain_per_ciphertext": ms_plain, "vs_plain": ms_plain / ms_batch,
+            "ms_plain_per_ciphertext_graph": ms_plain_graph, "vs_plain_graph": ms_plain_graph / ms_batch,
+            "plain_decrypts_ok": ok}
 
 
 def cpu_baseline_sample(seconds=None):
@@ -666,6 +752,8 @@ def main():
             line["cpu_baseline"] = cpu_baseline_sample()
         if not args.no_secondary:
             line["secondary"] = secondary_metrics(queue, peak)
+            line["secondary"]["bgv_enc_256_vs_plain_per_ciphertext"] = plain_encryption_comparison(
+                queue, q, p, s, key, msgs, ct)
         print(json.dumps(line), flush=True)
     queue.close()
     if world > 1:
