@@ -212,7 +212,7 @@ def bf16_peak_tflops():
         return 1900.0, "fallback"
 
 
-def dominant_roofline(q, transform_ms, per_transform, int_peak):
+def dominant_roofline(q, transform_ms, per_transform, int_peak, chacha_peak=None):
     """Roofline of the transform kernel that dominates a step (the fused
     CBD(10) -> NTT of the batch).  Tensor-core engine: algorithmic DRAM bytes
     and fp16 MMA flops per launch from the engine's own cost model, against
@@ -239,6 +239,23 @@ def dominant_roofline(q, transform_ms, per_transform, int_peak):
                        "peak_source": tensor_src + " (dense bf16; fp16 MMAs run at the same rate)"}
         primary, other, bound = ((hbm_view, tensor_view, "hbm") if hbm_view["frac"] >= tensor_view["frac"]
                                  else (tensor_view, hbm_view, "tensor"))
+        # per-resource bound of the whole transform: the sampling first group
+        # draws one ChaCha20 block per stage-0 pair (integer ALU, against the
+        # live block-rate probe) and writes its digit planes (9 words per
+        # element); the other groups' bytes and all MMA flops against HBM and
+        # the tensor peak (the larger; summing maxima per group would only
+        # raise the bound)
+        resource = None
+        if chacha_peak:
+            blocks = BATCH * N // 2
+            first_bytes = BATCH * N * 36
+            first_s = max(blocks / chacha_peak, first_bytes / (hbm * 1e9))
+            rest_s = max((cost["bytes"] - first_bytes) / (hbm * 1e9), cost["flops"] / (tensor_peak * 1e12))
+            resource = {"chacha_blocks_per_transform": blocks, "chacha_peak_blocks_per_s": chacha_peak,
+                        "chacha_peak_source": "measured live: hmpc_probe_chacha_rate",
+                        "first_group_bound_us": first_s * 1e6, "other_groups_bound_us": rest_s * 1e6,
+                        "transform_measured_us": transform_ms * 1e3,
+                        "frac": (first_s + rest_s) / (transform_ms * 1e-3)}
         return {
             "bound": bound,
             "kernel": "tc_group_kernel (tensor-core transform groups: fused CBD(10) sampler -> NTT, 256 x N=2^15, L=8)",
@@ -252,6 +269,7 @@ def dominant_roofline(q, transform_ms, per_transform, int_peak):
             "launches_per_transform": per_transform,
             "launch_ms": launch_ms,
             "plan": plan,
+            "resource_bound": resource,
         }
     butterflies = BATCH * (N // 2) * (N.bit_length() - 1)
     ops_per_launch = butterflies * mont_mul_ops(q.limbs) / per_transform
@@ -720,7 +738,7 @@ def main():
     barrier()
     transform_ms = k_start.elapsed_time(k_stop) / reps
     peak = queue.int_multiply_rate()
-    roofline = dominant_roofline(q, transform_ms, per_transform, peak)
+    roofline = dominant_roofline(q, transform_ms, per_transform, peak, queue.chacha_rate())
 
     if rank == 0:
         line = {

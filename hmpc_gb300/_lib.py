@@ -75,6 +75,7 @@ SIGNATURES = {
     "hmpc_context_synchronize": ([_vp], _int),
     "hmpc_context_launch_count": ([_vp, ctypes.POINTER(_u64)], _int),
     "hmpc_probe_int_multiply_rate": ([_vp, ctypes.POINTER(ctypes.c_double)], _int),
+    "hmpc_probe_chacha_rate": ([_vp, ctypes.POINTER(ctypes.c_double)], _int),
     "hmpc_modulus_create": ([_vp, _u32p, _int, ctypes.POINTER(_vp)], _int),
     "hmpc_modulus_destroy": ([_vp], _int),
     "hmpc_modulus_info": ([_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), _u32p], _int),

@@ -180,6 +180,12 @@ class Queue:
         _lib.call("hmpc_probe_int_multiply_rate", self.handle, ctypes.byref(out))
         return out.value
 
+    def chacha_rate(self):
+        """measured ChaCha20 blocks per second of the device (the samplers' ALU bound)"""
+        out = ctypes.c_double()
+        _lib.call("hmpc_probe_chacha_rate", self.handle, ctypes.byref(out))
+        return out.value
+
     def wait(self):
         """queue.wait() (hmpc/comp/queue.hpp:531-534)"""
         _lib.call("hmpc_context_synchronize", self.handle)

@@ -513,6 +513,20 @@ int hmpc_probe_int_multiply_rate(hmpc_context* ctx, double* ops_per_second)
     return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "integer multiply probe");
 }
 
+int hmpc_probe_chacha_rate(hmpc_context* ctx, double* blocks_per_second)
+{
+    if (int rc = enter(ctx))
+    {
+        return rc;
+    }
+    if (!blocks_per_second)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
+    }
+    cudaError_t e = probe_chacha_rate(ctx->stream, blocks_per_second);
+    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "ChaCha20 probe");
+}
+
 int hmpc_context_synchronize(hmpc_context* ctx)
 {
     if (int rc = enter(ctx))

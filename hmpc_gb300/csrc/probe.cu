@@ -2,6 +2,8 @@
 
 #include <cstdint>
 
+#include "chacha.cuh"
+
 namespace hmpc_gb300
 {
     namespace
@@ -41,6 +43,93 @@ namespace hmpc_gb300
                 sink[threadIdx.x] = acc;
             }
         }
+    }
+
+    namespace
+    {
+        constexpr int chacha_blocks_per_thread = 64;
+
+        // ChaCha20 blocks as the samplers compute them: one block per
+        // (key, nonce, counter), the first four output words consumed (a
+        // stage-0 pair of CBD(10) draws).  The nonce changes every iteration so
+        // that no quarter round of the first column round is loop-invariant
+        // (a sampler thread computes one block, where none can be hoisted).
+        __global__ void __launch_bounds__(256) chacha_kernel(RngKey k, uint32_t* sink)
+        {
+            const uint32_t counter0 = (blockIdx.x * blockDim.x + threadIdx.x) * chacha_blocks_per_thread;
+            uint32_t acc = 0;
+            for (int i = 0; i < chacha_blocks_per_thread; ++i)
+            {
+                RngKey ki = k;
+                ki.nonce[0] += static_cast<uint32_t>(i);
+                ki.nonce[1] ^= static_cast<uint32_t>(i) * 0x9e3779b9u;
+                ki.nonce[2] += static_cast<uint32_t>(i) << 7;
+                uint32_t out[16];
+                chacha20_block(ki, counter0 + static_cast<uint32_t>(i), out);
+                acc ^= out[0] ^ out[1] ^ out[2] ^ out[3];
+            }
+            if (acc == 0x12345678u)
+            {
+                sink[threadIdx.x] = acc;
+            }
+        }
+    }
+
+    cudaError_t probe_chacha_rate(cudaStream_t stream, double* blocks_per_second)
+    {
+        int device = 0, sms = 0;
+        cudaError_t e = cudaGetDevice(&device);
+        if (e == cudaSuccess)
+        {
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        }
+        if (e != cudaSuccess)
+        {
+            return e;
+        }
+        uint32_t* sink = nullptr;
+        if ((e = cudaMalloc(&sink, 256 * sizeof(uint32_t))) != cudaSuccess)
+        {
+            return e;
+        }
+        RngKey k{};
+        for (int i = 0; i < 8; ++i)
+        {
+            k.key[i] = 0x01234567u * static_cast<uint32_t>(i + 1);
+        }
+        const unsigned blocks = static_cast<unsigned>(sms) * 8u;
+        cudaEvent_t start, stop;
+        cudaEventCreate(&start);
+        cudaEventCreate(&stop);
+        float best = 1e30f;
+        for (int rep = 0; rep < 6; ++rep)
+        {
+            k.nonce[0] = static_cast<uint32_t>(rep);
+            cudaEventRecord(start, stream);
+            chacha_kernel<<<blocks, 256, 0, stream>>>(k, sink);
+            cudaEventRecord(stop, stream);
+            e = cudaEventSynchronize(stop);
+            if (e != cudaSuccess)
+            {
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, start, stop);
+            if (rep > 0 && ms < best)
+            {
+                best = ms;
+            }
+        }
+        cudaEventDestroy(start);
+        cudaEventDestroy(stop);
+        cudaFree(sink);
+        if (e != cudaSuccess)
+        {
+            return e;
+        }
+        const double count = static_cast<double>(blocks) * 256.0 * chacha_blocks_per_thread;
+        *blocks_per_second = count / (static_cast<double>(best) * 1e-3);
+        return cudaSuccess;
     }
 
     cudaError_t probe_int_multiply_rate(cudaStream_t stream, double* ops_per_second)

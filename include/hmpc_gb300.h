@@ -69,6 +69,11 @@ int hmpc_context_launch_count(const hmpc_context* ctx, uint64_t* count);
  * operations per second (mad.lo and mad.hi each count one): the denominator of
  * the integer-pipe roofline.  No counterpart in the reference. */
 int hmpc_probe_int_multiply_rate(hmpc_context* ctx, double* ops_per_second);
+/* Measured ChaCha20 block rate of the context's device (20 rounds, one block
+ * per (key, nonce, counter), four output words used, no memory traffic): the
+ * denominator of the integer-ALU roofline of the fused samplers.  No
+ * counterpart in the reference. */
+int hmpc_probe_chacha_rate(hmpc_context* ctx, double* blocks_per_second);
 /* hmpc::comp::queue::wait (hmpc/comp/queue.hpp:531-534) */
 int hmpc_context_synchronize(hmpc_context* ctx);
 
