@@ -4,6 +4,8 @@
   python -m hmpc_gb300.workloads ntt --n 4096 --batch 1 --q ntt
   python -m hmpc_gb300.workloads fma --elements 16777216
   python -m hmpc_gb300.workloads bgv --batch 256
+  python -m hmpc_gb300.workloads matvec --n 32768 --batch 16 --rows 4 --cols 4
+  python -m hmpc_gb300.workloads sum --elements 16777216
 
 Each runs the operation `--reps` times on cuda:0 and prints the mean time of
 the repetitions after the first (CUDA events on the queue's stream).
@@ -66,7 +68,10 @@ def timed(queue, fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["ntt", "intt", "ntt-cbd", "ntt-uniform", "fma", "bgv", "plain-ntt"])
+    ap.add_argument("workload", choices=["ntt", "intt", "ntt-cbd", "ntt-uniform", "fma", "bgv", "plain-ntt", "matvec",
+                                         "sum", "ntt-intt"])
+    ap.add_argument("--rows", type=int, default=4)
+    ap.add_argument("--cols", type=int, default=4)
     ap.add_argument("--n", type=int, default=1 << 15)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--q", default="q256")
@@ -82,7 +87,31 @@ def main(argv=None):
     queue = Queue(key=KEY)
     q = queue.modulus(MODULI[args.q])
     result = {"workload": args.workload, "q_limbs": q.limbs}
-    if args.workload in ("ntt", "intt", "ntt-cbd", "ntt-uniform", "plain-ntt"):
+    if args.workload == "ntt-intt":
+        # examples/ntt.cpp: one forward then one inverse transform
+        q.prepare(args.n)
+        if args.tune:
+            q.tune(args.n, args.batch)
+            q.tune(args.n, args.batch, inverse=True)
+        x = queue.uniform(q, (args.batch,), args.n)
+        y, z = Tensor(q, (args.batch,), args.n), Tensor(q, (args.batch,), args.n)
+        ms = timed(queue, lambda: (queue.ntt(x, out=y), queue.intt(y, out=z)), args.reps)
+        result.update(n=args.n, batch=args.batch, ms=ms, tile=q.plan(args.n, args.batch),
+                      tile_inverse=q.plan(args.n, args.batch, inverse=True))
+    elif args.workload == "matvec":
+        # batch x (rows x cols) matrices of NTT-form polynomials times cols-vectors
+        m = queue.uniform(q, (args.batch, args.rows, args.cols), args.n)
+        x = queue.uniform(q, (args.batch, args.cols), args.n)
+        z = Tensor(q, (args.batch, args.rows), args.n)
+        ms = timed(queue, lambda: queue.matrix_vector_product(m, x, out=z), args.reps)
+        result.update(n=args.n, batch=args.batch, rows=args.rows, cols=args.cols, ms=ms)
+    elif args.workload == "sum":
+        q = queue.modulus(MODULI["fma"])
+        result["q_limbs"] = q.limbs
+        x = queue.uniform(q, (args.elements,))
+        ms = timed(queue, lambda: queue.sum(x), args.reps)
+        result.update(elements=args.elements, ms=ms, gbs=args.elements * 4 * q.limbs / (ms * 1e-3) / 1e9)
+    elif args.workload in ("ntt", "intt", "ntt-cbd", "ntt-uniform", "plain-ntt"):
         q.prepare(args.n)
         if args.tune:
             result["tuned_ms"] = q.tune(args.n, args.batch, inverse=args.workload == "intt")
