@@ -93,6 +93,9 @@ def main(argv=None):
         if args.tune:
             q.tune(args.n, args.batch)
             q.tune(args.n, args.batch, inverse=True)
+        elif args.radix_bits is not None:
+            for inverse in (False, True):
+                q.set_plan(args.n, args.batch, inverse, args.radix_bits, args.local_bits, args.col_bits)
         x = queue.uniform(q, (args.batch,), args.n)
         y, z = Tensor(q, (args.batch,), args.n), Tensor(q, (args.batch,), args.n)
         ms = timed(queue, lambda: (queue.ntt(x, out=y), queue.intt(y, out=z)), args.reps)
