@@ -359,6 +359,57 @@ namespace hmpc_gb300
         asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(tc::smem_u32(p)), "r"(a), "r"(b) : "memory");
     }
 
+    // The pair of centred binomial values of one stage-0 generator: the first
+    // ceil(2V/32) keystream words for the first sample, the next as many for
+    // the second, the top word of each masked to 2V mod 32 bits, popcount - V'
+    // with V' = 2V / 2 (hmpc/random/binomial.hpp:29-86,110-122).  BGV's two
+    // variances (2V = 1 for the secret and u, 2V = 20 for the noise) take
+    // compile-time word counts, so only the keystream words they consume are
+    // computed and the masks fold away; other variances draw eight words.
+    __device__ __forceinline__ void tc_cbd_pair(const TcGroupParams& p, uint32_t counter, int& a, int& b)
+    {
+        if (p.vx2 == 20)
+        {
+            uint32_t w[4];
+            chacha_stream<4>(p.rng, counter, w);
+            a = __popc(w[0]) + __popc(w[1] & 0xffu) - 20;
+            b = __popc(w[2]) + __popc(w[3] & 0xffu) - 20;
+            return;
+        }
+        if (p.vx2 == 1)
+        {
+            uint32_t w[2];
+            chacha_stream<2>(p.rng, counter, w);
+            a = __popc(w[0] & 3u) - 1;
+            b = __popc(w[1] & 3u) - 1;
+            return;
+        }
+        const int count = 2 * static_cast<int>(p.vx2);
+        const int nw = static_cast<int>(p.nw);
+        uint32_t w[8];
+        chacha_stream<8>(p.rng, counter, w);
+        a = 0;
+        b = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+        {
+            const int iv = i - nw;  // word of the second sample
+            uint32_t mu = 0u, mv = 0u;
+            if (i < nw)
+            {
+                mu = (i == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
+            }
+            else if (iv < nw)
+            {
+                mv = (iv == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
+            }
+            a += __popc(w[i] & mu);
+            b += __popc(w[i] & mv);
+        }
+        a -= static_cast<int>(p.vx2);
+        b -= static_cast<int>(p.vx2);
+    }
+
     // first forward group fed by centred binomial samples: r = 8, stage-0 pairs
     // (m, m + 4) of a row come from one generator with counter = poly * N +
     // index of the first element, first draw for m, second for m + 4
@@ -372,30 +423,8 @@ namespace hmpc_gb300
         int e_u = 0, e_v = 0;
         if (r.ok)
         {
-            const int count = 2 * static_cast<int>(p.vx2);
-            const int nw = static_cast<int>(p.nw);
             const uint64_t idx = r.base + (static_cast<uint64_t>(part) << p.lo);
-            uint32_t w[8];
-            chacha_stream<8>(p.rng, static_cast<uint32_t>(idx), w);
-            int a = 0, b = 0;
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-            {
-                const int iv = i - nw;  // word of the second sample
-                uint32_t mu = 0u, mv = 0u;
-                if (i < nw)
-                {
-                    mu = (i == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
-                }
-                else if (iv < nw)
-                {
-                    mv = (iv == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
-                }
-                a += __popc(w[i] & mu);
-                b += __popc(w[i] & mv);
-            }
-            e_u = a - static_cast<int>(p.vx2);
-            e_v = b - static_cast<int>(p.vx2);
+            tc_cbd_pair(p, static_cast<uint32_t>(idx), e_u, e_v);
         }
         uint8_t* seg = sa + tc::operand_offset(row, 0, tc_rows);
         const __half hu = __int2half_rn(e_u), hv = __int2half_rn(e_v);
@@ -448,8 +477,6 @@ namespace hmpc_gb300
         __int128 x[2] = {0, 0};
         if (r.ok)
         {
-            const int count = 2 * static_cast<int>(p.vx2);
-            const int nw = static_cast<int>(p.nw);
             const uint64_t idx = r.base + (static_cast<uint64_t>(part) << p.lo);
             // the plaintext loads go out before the keystream is computed, so
             // their latency hides behind it
@@ -464,28 +491,11 @@ namespace hmpc_gb300
                     msg[j][1] = p.msg_limbs > 1 ? __ldcs(p.msg + p.msg_stride + e) : 0u;
                 }
             }
-            uint32_t w[8];
-            chacha_stream<8>(p.rng, static_cast<uint32_t>(idx), w);
             int a = 0, b = 0;
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-            {
-                const int iv = i - nw;
-                uint32_t mu = 0u, mv = 0u;
-                if (i < nw)
-                {
-                    mu = (i == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
-                }
-                else if (iv < nw)
-                {
-                    mv = (iv == nw - 1 && (count & 31)) ? (1u << (count & 31)) - 1u : 0xffffffffu;
-                }
-                a += __popc(w[i] & mu);
-                b += __popc(w[i] & mv);
-            }
+            tc_cbd_pair(p, static_cast<uint32_t>(idx), a, b);
             const uint64_t pval = p.pq[0] | (p.msg_limbs > 1 ? static_cast<uint64_t>(p.pq[1]) << 32 : 0ull);
-            x[0] = static_cast<__int128>(pval) * (a - static_cast<int>(p.vx2));
-            x[1] = static_cast<__int128>(pval) * (b - static_cast<int>(p.vx2));
+            x[0] = static_cast<__int128>(pval) * a;
+            x[1] = static_cast<__int128>(pval) * b;
             if (p.msg)
             {
                 x[0] += tc_centred_lift(p, msg[0]);
