@@ -722,6 +722,22 @@ def main():
     back = lhe.Ciphertext(Tensor(q, (BATCH,), N, host_c0.to(queue.device)), Tensor(q, (BATCH,), N,
                                                                                host_c1.to(queue.device)))
     ok = bool((lhe.dec(queue, s, back, p).data == msgs.data).all().item())
+    # the host link's pinned copy rates on this machine, each direction alone on
+    # its copy stream: the copies of a step bound e2e at BATCH / max(in, out)
+    link = {}
+    for name, st, dst, src in (("h2d", copy_in, sets[0]["msgs"].data, host_msgs),
+                               ("d2h", copy_out, host_c0, sets[0]["ct"].c0.data)):
+        c_start, c_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st):
+            dst.copy_(src, non_blocking=True)
+            c_start.record(st)
+            for _ in range(3):
+                dst.copy_(src, non_blocking=True)
+            c_stop.record(st)
+        c_stop.synchronize()
+        link[name] = 3 * src.numel() * 4 / (c_start.elapsed_time(c_stop) * 1e-3) / 1e9
+    copy_s = max(host_msgs.numel() * 4 / (link["h2d"] * 1e9),
+                 (host_c0.numel() + host_c1.numel()) * 4 / (link["d2h"] * 1e9))
 
     # ------------------------------------------- dominant kernel roofline
     # the fused CBD(10) -> NTT over the batch: the transform's kernel launches
@@ -761,6 +777,8 @@ def main():
                 "h2d_bytes_per_step": host_msgs.numel() * 4,
                 "d2h_bytes_per_step": (host_c0.numel() + host_c1.numel()) * 4,
                 "decrypts_ok": ok,
+                "link_gbs": link,
+                "copy_bound": BATCH / copy_s,
             },
             "gpu_launches": launches,
             "roofline": roofline,
