@@ -578,6 +578,11 @@ def cpu_baseline_sample(seconds=None):
         elapsed += time.perf_counter() - t0
         nonce = oracle.nonce_add(nonce, 3 * N * per)
         done += per
+    # the same on one core: one batch of two encryptions
+    one = 2
+    t0 = time.perf_counter()
+    oracle.lhe_enc(q, p, N, one, a, b, msgs[:, : N * one], False, SEED_KEY, nonce, threads=1)
+    one_s = time.perf_counter() - t0
     return {
         "value": done / elapsed,
         "unit": "encryptions/s",
@@ -585,6 +590,7 @@ def cpu_baseline_sample(seconds=None):
         "kind": "port",
         "sample": f"{done} encryptions ({done // per} batches of {per}) at N=2^15, q 256-bit, CPU oracle "
                   f"(reference algorithm restated, OpenMP), {elapsed:.1f} s",
+        "one_core": {"value": one / one_s, "cores": 1, "sample": f"{one} encryptions, {one_s:.2f} s"},
     }
 
 
