@@ -52,6 +52,32 @@ CONFIG = {
 DOMINANT_TRAFFIC_BYTES = 711.9e6
 
 
+def rate_probes():
+    """The device's live rate probes (libhmpc_gb300_probes.so, a measurement
+    library built beside the product library): 32-bit multiplies per second
+    and ChaCha20 blocks per second, the denominators of the integer-pipe and
+    integer-ALU rooflines."""
+    import ctypes
+
+    import torch
+
+    from hmpc_gb300 import build as _build
+
+    lib = ctypes.CDLL(str(_build.PROBES))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rates = {}
+    for name in ("int_multiply_rate", "chacha_rate"):
+        fn = getattr(lib, "hmpc_bench_" + name)
+        fn.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+        fn.restype = ctypes.c_int
+        out = ctypes.c_double()
+        rc = fn(stream, ctypes.byref(out))
+        if rc:
+            raise RuntimeError(f"rate probe {name} failed with CUDA error {rc}")
+        rates[name] = out.value
+    return rates
+
+
 def mont_mul_ops(limbs):
     """32-bit multiply operations of one L-limb Montgomery product:
     L^2 lo/hi product pairs plus L(L+1) reduction products (4L^2 + L)"""
@@ -252,7 +278,7 @@ def dominant_roofline(q, transform_ms, per_transform, int_peak, chacha_peak=None
             first_s = max(blocks / chacha_peak, first_bytes / (hbm * 1e9))
             rest_s = max((cost["bytes"] - first_bytes) / (hbm * 1e9), cost["flops"] / (tensor_peak * 1e12))
             resource = {"chacha_blocks_per_transform": blocks, "chacha_peak_blocks_per_s": chacha_peak,
-                        "chacha_peak_source": "measured live: hmpc_probe_chacha_rate",
+                        "chacha_peak_source": "measured live: hmpc_bench_chacha_rate",
                         "first_group_bound_us": first_s * 1e6, "other_groups_bound_us": rest_s * 1e6,
                         "transform_measured_us": transform_ms * 1e3,
                         "frac": (first_s + rest_s) / (transform_ms * 1e-3)}
@@ -283,7 +309,7 @@ def dominant_roofline(q, transform_ms, per_transform, int_peak, chacha_peak=None
         "unit": "T int32-mul/s",
         "frac": achieved / int_peak,
         "traffic": None,
-        "peak_source": "measured live: hmpc_probe_int_multiply_rate (independent mad.lo/mad.hi chains)",
+        "peak_source": "measured live: hmpc_bench_int_multiply_rate (independent mad.lo/mad.hi chains)",
         "hbm_view": {"achieved": algorithmic_bytes / launch_s / 1e9, "peak": hbm, "unit": "GB/s",
                      "frac": algorithmic_bytes / launch_s / 1e9 / hbm, "peak_source": hbm_src},
         "launch_ms": launch_ms,
@@ -302,7 +328,7 @@ def secondary_metrics(queue, int_peak):
     from hmpc_gb300 import _lib
     from hmpc_gb300.batch import NttBatch, uneven_degrees
     from hmpc_gb300.comp import Tensor
-    from hmpc_gb300.workloads import MODULI
+    from hmpc_gb300.moduli import MODULI
 
     out = {}
     stream = queue.stream
@@ -594,7 +620,146 @@ def cpu_baseline_sample(seconds=None):
     }
 
 
+WORKLOADS = ["ntt", "intt", "ntt-cbd", "ntt-uniform", "fma", "bgv", "plain-ntt", "matvec", "sum", "ntt-intt",
+             "batched"]
+
+
+def workload_main(argv):
+    """One named workload on cuda:0 (the commands of the profile summaries):
+    runs the operation `--reps` times and prints the mean time of the
+    repetitions after the first (CUDA events on the queue's stream).
+
+      python bench.py --workload ntt-cbd --n 32768 --batch 256 --vx2 20 --reps 2 --radix-bits 0 --local-bits 1
+      python bench.py --workload batched --reps 3
+    """
+    import torch
+
+    from hmpc_gb300 import lhe
+    from hmpc_gb300.comp import Queue, Tensor
+    from hmpc_gb300.moduli import MODULI
+
+    ap = argparse.ArgumentParser(prog="bench.py --workload")
+    ap.add_argument("--workload", choices=WORKLOADS, required=True)
+    ap.add_argument("--rows", type=int, default=4)
+    ap.add_argument("--cols", type=int, default=4)
+    ap.add_argument("--n", type=int, default=1 << 15)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--q", default="q256")
+    ap.add_argument("--vx2", type=int, default=20)
+    ap.add_argument("--elements", type=int, default=1 << 24)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--tune", action="store_true", help="autotune the tile shape first")
+    ap.add_argument("--radix-bits", type=int, default=None,
+                    help="force a tile shape (with --local-bits, --col-bits); 0 = tensor-core engine")
+    ap.add_argument("--local-bits", type=int, default=0)
+    ap.add_argument("--col-bits", type=int, default=4)
+    args = ap.parse_args(argv)
+
+    def timed(fn, reps):
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fn()
+        queue.wait()
+        start.record(queue.stream)
+        for _ in range(max(0, reps - 1)):
+            fn()
+        stop.record(queue.stream)
+        queue.wait()
+        return start.elapsed_time(stop) / max(1, reps - 1)
+
+    queue = Queue(key=SEED_KEY)
+    q = queue.modulus(MODULI[args.q])
+    w = args.workload
+    result = {"workload": w, "q_limbs": q.limbs}
+
+    def plan(inverse):
+        if args.tune:
+            return q.tune(args.n, args.batch, inverse=inverse)
+        if args.radix_bits is not None:
+            q.set_plan(args.n, args.batch, inverse, args.radix_bits, args.local_bits, args.col_bits)
+        return None
+
+    if w == "ntt-intt":
+        # examples/ntt.cpp: one forward then one inverse transform
+        q.prepare(args.n)
+        plan(False)
+        plan(True)
+        x = queue.uniform(q, (args.batch,), args.n)
+        y, z = Tensor(q, (args.batch,), args.n), Tensor(q, (args.batch,), args.n)
+        ms = timed(lambda: (queue.ntt(x, out=y), queue.intt(y, out=z)), args.reps)
+        result.update(n=args.n, batch=args.batch, ms=ms, tile=q.plan(args.n, args.batch),
+                      tile_inverse=q.plan(args.n, args.batch, inverse=True))
+    elif w == "matvec":
+        # batch x (rows x cols) matrices of NTT-form polynomials times cols-vectors
+        m = queue.uniform(q, (args.batch, args.rows, args.cols), args.n)
+        x = queue.uniform(q, (args.batch, args.cols), args.n)
+        z = Tensor(q, (args.batch, args.rows), args.n)
+        ms = timed(lambda: queue.matrix_vector_product(m, x, out=z), args.reps)
+        result.update(n=args.n, batch=args.batch, rows=args.rows, cols=args.cols, ms=ms)
+    elif w in ("sum", "fma"):
+        q = queue.modulus(MODULI["fma"])
+        result["q_limbs"] = q.limbs
+        if w == "sum":
+            x = queue.uniform(q, (args.elements,))
+            ms = timed(lambda: queue.sum(x), args.reps)
+            moved = args.elements * 4 * q.limbs
+        else:
+            a, b, c = (queue.uniform(q, (args.elements,)) for _ in range(3))
+            d = Tensor(q, (args.elements,))
+            ms = timed(lambda: queue.fma(a, b, c, out=d), args.reps)
+            moved = args.elements * 16 * q.limbs
+        result.update(elements=args.elements, ms=ms, gbs=moved / (ms * 1e-3) / 1e9)
+    elif w == "batched":
+        # the uneven batch of the batched configuration: 512 polynomials of
+        # degrees 2^12..2^16 mod the 192-bit prime, one persistent launch
+        from hmpc_gb300.batch import NttBatch, uneven_degrees
+
+        qb = queue.modulus(MODULI["q192"])
+        degrees = uneven_degrees(512)
+        xs = [queue.uniform(qb, (), n) for n in degrees]
+        ys = [Tensor(qb, (), n) for n in degrees]
+        batch = NttBatch(queue, qb, degrees, autotune=args.tune)
+        ms = timed(lambda: batch.run(xs, ys), args.reps)
+        result.update(q_limbs=qb.limbs, polynomials=len(degrees), coefficients=sum(degrees), ms=ms,
+                      tile=batch.info())
+        batch.close()
+    elif w in ("ntt", "intt", "ntt-cbd", "ntt-uniform", "plain-ntt"):
+        q.prepare(args.n)
+        tuned = plan(w == "intt")
+        if tuned is not None:
+            result["tuned_ms"] = tuned
+        result["tile"] = q.plan(args.n, args.batch, inverse=w == "intt")
+        x = queue.uniform(q, (args.batch,), args.n)
+        out = Tensor(q, (args.batch,), args.n)
+        fn = {
+            "ntt": lambda: queue.ntt(x, out=out),
+            "intt": lambda: queue.intt(x, out=out),
+            "ntt-cbd": lambda: queue.ntt_centered_binomial(q, args.n, (args.batch,), args.vx2, out=out),
+            "ntt-uniform": lambda: queue.ntt_uniform(q, args.n, (args.batch,), out=out),
+            "plain-ntt": lambda: queue.ntt_plain(x, out=out),
+        }[w]
+        result.update(n=args.n, batch=args.batch, ms=timed(fn, args.reps))
+    elif w == "bgv":
+        p = queue.modulus(MODULI["p64"])
+        q.prepare(args.n)
+        p.prepare(args.n)
+        tuned = plan(False)
+        if tuned is not None:
+            result["tuned_ms"] = tuned
+            p.tune(args.n, args.batch, inverse=True)
+        result["tile"] = q.plan(args.n, args.batch)
+        s, key = lhe.keygen(queue, q, p, args.n)
+        msgs = queue.uniform(p, (args.batch,), args.n)
+        ct = lhe.Ciphertext(Tensor(q, (args.batch,), args.n), Tensor(q, (args.batch,), args.n))
+        ms = timed(lambda: lhe.enc(queue, key, msgs, q, out=ct), args.reps)
+        result.update(n=args.n, batch=args.batch, ms=ms, enc_per_s=args.batch / (ms * 1e-3))
+    print(json.dumps(result))
+    queue.close()
+
+
 def main():
+    if "--workload" in sys.argv[1:]:
+        workload_main(sys.argv[1:])
+        return
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -759,8 +924,9 @@ def main():
     k_stop.record(stream)
     barrier()
     transform_ms = k_start.elapsed_time(k_stop) / reps
-    peak = queue.int_multiply_rate()
-    roofline = dominant_roofline(q, transform_ms, per_transform, peak, queue.chacha_rate())
+    rates = rate_probes()
+    peak = rates["int_multiply_rate"]
+    roofline = dominant_roofline(q, transform_ms, per_transform, peak, rates["chacha_rate"])
 
     if rank == 0:
         line = {

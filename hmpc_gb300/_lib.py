@@ -74,8 +74,6 @@ SIGNATURES = {
     "hmpc_context_set_nonce": ([_vp, _u32p], _int),
     "hmpc_context_synchronize": ([_vp], _int),
     "hmpc_context_launch_count": ([_vp, ctypes.POINTER(_u64)], _int),
-    "hmpc_probe_int_multiply_rate": ([_vp, ctypes.POINTER(ctypes.c_double)], _int),
-    "hmpc_probe_chacha_rate": ([_vp, ctypes.POINTER(ctypes.c_double)], _int),
     "hmpc_modulus_create": ([_vp, _u32p, _int, ctypes.POINTER(_vp)], _int),
     "hmpc_modulus_destroy": ([_vp], _int),
     "hmpc_modulus_info": ([_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), _u32p], _int),
@@ -84,6 +82,8 @@ SIGNATURES = {
     "hmpc_modulus_set_plan": ([_vp, _u64, _u64, _int, _int, _int, _int], _int),
     "hmpc_modulus_get_plan": ([_vp, _u64, _u64, _int] + [ctypes.POINTER(_int)] * 3, _int),
     "hmpc_modulus_tc_cost": ([_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(TcCost)], _int),
+    "hmpc_modulus_tc_column_max": ([_vp, _u64, _int, _int, _u32p], _int),
+    "hmpc_context_set_tc_column_bound": ([_vp, ctypes.c_uint32], _int),
     "hmpc_wire_layout": ([ctypes.POINTER(WireMessage), _u64, ctypes.c_uint8, ctypes.POINTER(_u64),
                           ctypes.POINTER(_u64)], _int),
     "hmpc_wire_pack": ([_vp, ctypes.POINTER(WireMessage), _u64, ctypes.c_uint8, ctypes.c_char_p,

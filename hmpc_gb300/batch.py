@@ -60,7 +60,7 @@ def uneven_degrees(count, log_min=12, log_max=16, seed=0):
     stream (one word per polynomial, reduced modulo the number of choices)."""
     import struct
 
-    from .workloads import chacha20_words
+    from .moduli import chacha20_words
 
     words = chacha20_words([seed] + [0] * 7, count)
     choices = log_max - log_min + 1

@@ -2,7 +2,8 @@
 
 One translation unit per limb count (kernels.cu with -DHMPC_L=1..9) plus the
 host-side C-ABI layer; the units compile in parallel and only the ones whose
-sources changed are rebuilt.
+sources changed are rebuilt.  The benchmark's rate probes (probe.cu) link into
+a library of their own, libhmpc_gb300_probes.so, outside the product's ABI.
 """
 import concurrent.futures
 import os
@@ -14,6 +15,7 @@ HERE = pathlib.Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = OUT / "libhmpc_gb300.so"
+PROBES = OUT / "libhmpc_gb300_probes.so"
 INCLUDE = HERE.parent / "include"
 LIMBS = range(1, 10)
 TC_LIMBS = (2, 4, 8)  # limb counts of the tensor-core transform
@@ -61,7 +63,10 @@ def build(verbose=False, jobs=None):
         objects.append(obj)
         if _stale(obj, [CSRC / "tensor_ntt.cu", *headers]):
             steps.append(common + [f"-DHMPC_L={limbs}", "-c", str(CSRC / "tensor_ntt.cu"), "-o", str(obj)])
-    for name in ("api.cpp", "host_math.cpp", "probe.cu", "noalloc.cu", "batched.cpp", "serve.cpp", "cipher.cu",
+    probe_obj = OUT / "probe.o"
+    if _stale(probe_obj, [CSRC / "probe.cu", *headers]):
+        steps.append(common + ["-c", str(CSRC / "probe.cu"), "-o", str(probe_obj)])
+    for name in ("api.cpp", "host_math.cpp", "noalloc.cu", "batched.cpp", "serve.cpp", "cipher.cu",
                  "tc.cpp", "wire.cu", "linalg.cpp"):
         obj = OUT / (name.rsplit(".", 1)[0] + ".o")
         objects.append(obj)
@@ -74,6 +79,8 @@ def build(verbose=False, jobs=None):
                 print(log)
     if steps or _stale(LIB, objects):
         _run([nvcc(), "-shared", *ARCH, "-o", str(LIB), *map(str, objects), "-lcudart"])
+    if _stale(PROBES, [probe_obj]):
+        _run([nvcc(), "-shared", *ARCH, "-o", str(PROBES), str(probe_obj), "-lcudart"])
     return LIB
 
 

@@ -67,6 +67,12 @@ class Modulus:
                   ctypes.byref(cb))
         return {"radix_bits": r.value, "local_bits": lb.value, "col_bits": cb.value}
 
+    def tc_column_max(self, n, inverse=False, splits=1):
+        """largest column sum of |digit| of the tensor-core constants of (n, direction, splits)"""
+        out = ctypes.c_uint32()
+        _lib.call("hmpc_modulus_tc_column_max", self.handle, n, int(inverse), splits, ctypes.byref(out))
+        return out.value
+
     def tc_cost(self, n, batch, inverse=False, producer=_lib.PRODUCER_TENSOR, splits=1):
         """launches, algorithmic DRAM bytes and MMA flops of one tensor-core transform"""
         out = _lib.TcCost()
@@ -174,17 +180,9 @@ class Queue:
         _lib.call("hmpc_context_launch_count", self.handle, ctypes.byref(out))
         return out.value
 
-    def int_multiply_rate(self):
-        """measured 32-bit multiply operations per second of the device"""
-        out = ctypes.c_double()
-        _lib.call("hmpc_probe_int_multiply_rate", self.handle, ctypes.byref(out))
-        return out.value
-
-    def chacha_rate(self):
-        """measured ChaCha20 blocks per second of the device (the samplers' ALU bound)"""
-        out = ctypes.c_double()
-        _lib.call("hmpc_probe_chacha_rate", self.handle, ctypes.byref(out))
-        return out.value
+    def set_tc_column_bound(self, bound):
+        """lower the tensor-core engine's column bound for constants built afterwards"""
+        _lib.call("hmpc_context_set_tc_column_bound", self.handle, int(bound))
 
     def wait(self):
         """queue.wait() (hmpc/comp/queue.hpp:531-534)"""

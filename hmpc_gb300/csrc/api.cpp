@@ -16,7 +16,6 @@
 #include "host_math.hpp"
 #include "internal.hpp"
 #include "plan.hpp"
-#include "probe.hpp"
 
 using namespace hmpc_gb300;
 
@@ -499,34 +498,6 @@ int hmpc_context_launch_count(const hmpc_context* ctx, uint64_t* count)
     return HMPC_OK;
 }
 
-int hmpc_probe_int_multiply_rate(hmpc_context* ctx, double* ops_per_second)
-{
-    if (int rc = enter(ctx))
-    {
-        return rc;
-    }
-    if (!ops_per_second)
-    {
-        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
-    }
-    cudaError_t e = probe_int_multiply_rate(ctx->stream, ops_per_second);
-    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "integer multiply probe");
-}
-
-int hmpc_probe_chacha_rate(hmpc_context* ctx, double* blocks_per_second)
-{
-    if (int rc = enter(ctx))
-    {
-        return rc;
-    }
-    if (!blocks_per_second)
-    {
-        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null output");
-    }
-    cudaError_t e = probe_chacha_rate(ctx->stream, blocks_per_second);
-    return e == cudaSuccess ? HMPC_OK : cuda_fail(e, "ChaCha20 probe");
-}
-
 int hmpc_context_synchronize(hmpc_context* ctx)
 {
     if (int rc = enter(ctx))
@@ -680,6 +651,37 @@ int hmpc_modulus_tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inve
         return rc;
     }
     return tc_cost(mod, n, batch, inverse != 0, producer_kind, splits, out);
+}
+
+int hmpc_modulus_tc_column_max(hmpc_modulus* mod, uint64_t n, int inverse, int splits, uint32_t* out)
+{
+    if (!mod || !out)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null argument");
+    }
+    if (int rc = enter(mod->ctx))
+    {
+        return rc;
+    }
+    if (int rc = check_degree(n))
+    {
+        return rc;
+    }
+    return tc_column_max(mod->ctx, mod, n, inverse != 0, splits, out);
+}
+
+int hmpc_context_set_tc_column_bound(hmpc_context* ctx, uint32_t bound)
+{
+    if (!ctx)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null context");
+    }
+    if (bound > tc_byte_carry_column_bound)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "the two-operation carry is exact up to a column bound of 32512");
+    }
+    ctx->tc_column_bound = bound;
+    return HMPC_OK;
 }
 
 int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits,

@@ -54,7 +54,15 @@ namespace hmpc_gb300::detail
         // false: a group's constants exceed the two-operation carry's range and
         // this (modulus, degree, direction) runs on the CUDA cores
         bool fit = true;
+        // the largest sum of |digit| over one column of the digit-fed groups' images
+        uint32_t column_max = 0;
     };
+
+    // The carry of a group fed by digits takes two operations per digit while
+    // every column sum stays within (-2^22 + 2^15, 2^22 - 2^15); with digits
+    // |x| <= 128 that holds when each constant column's sum of |digit| is at
+    // most this bound (about twice what balanced random digits give)
+    constexpr uint32_t tc_byte_carry_column_bound = 32512;
 
     // first group of a forward transform fed by x = p * CBD(V) + lift(m):
     // plaintext residues m mod p (nullptr: none) and the plaintext modulus
@@ -92,6 +100,10 @@ struct hmpc_context
     uint64_t tc_workspace_words = 0;
     uint32_t* tc_error = nullptr;
     int sm_count = 0;
+    // column bound the tensor-core engine accepts for constants built through
+    // this context (at most tc_byte_carry_column_bound; lowered only by tests
+    // of the refusal)
+    uint32_t tc_column_bound = hmpc_gb300::detail::tc_byte_carry_column_bound;
     // a second stream for independent work of one call (fork / join events)
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t fork_event = nullptr;
@@ -198,6 +210,13 @@ struct hmpc_modulus
     std::map<std::tuple<int, int, uint64_t>, TileChoice> tile_choices;
     std::mutex tables_mutex;  // the serving thread looks tables up while clients register new degrees
 
+    // whether the twiddle tables of degree n exist (no allocation)
+    bool has_tables(uint64_t n)
+    {
+        std::lock_guard<std::mutex> lock(tables_mutex);
+        return tables.find(n) != tables.end();
+    }
+
     int prepare(uint64_t n, hmpc_gb300::detail::Tables** out)
     {
         std::lock_guard<std::mutex> lock(tables_mutex);
@@ -269,4 +288,7 @@ namespace hmpc_gb300::detail
     int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
                        int count, uint32_t* out, int splits);
     int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out);
+    // builds (once) the constants of the transform (n, direction, splits) and
+    // reports their largest column sum of |digit|
+    int tc_column_max(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, int splits, uint32_t* out);
 }

@@ -7,7 +7,10 @@
 // latency-critical loop that must not pay the implicit device-wide
 // synchronisation that cudaMalloc and cudaFree can trigger.  For them,
 // hmpc_lhe_enc_noalloc takes its intermediates from one fixed array in device
-// memory that is part of this library's image.
+// memory that is part of this library's image.  Its transforms always run on
+// the CUDA-core tiles (the tensor-core engine keeps digit buffers and constant
+// images of its own, which it allocates), in the reference's four-transform
+// order; the ciphertexts are bit-identical to hmpc_lhe_enc's on either engine.
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -75,16 +78,21 @@ extern "C" int hmpc_lhe_enc_noalloc(hmpc_context* ctx, hmpc_modulus* q, hmpc_mod
         return HMPC_OK;
     }
     // the transforms must not build (and allocate) twiddle tables here
-    if (q->tables.find(n) == q->tables.end() || (plaintext_ntt && p->tables.find(n) == p->tables.end()))
+    if (!q->has_tables(n) || (plaintext_ntt && !p->has_tables(n)))
     {
         return fail(HMPC_ERROR_INVALID_ARGUMENT,
                     "twiddle tables for this degree are not built: call hmpc_modulus_prepare(q, n) (and "
                     "hmpc_modulus_prepare(p, n) for NTT-form plaintexts) before the allocation-free encryption");
     }
+    // bound the batch before forming n * batch, which could wrap otherwise
+    if (batch > noalloc_scratch_words / n)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "batch too large for the allocation-free encryption");
+    }
     const uint64_t elements = n * batch;
     const uint64_t lq = static_cast<uint64_t>(q->c.limbs);
     const uint64_t lp = static_cast<uint64_t>(p->c.limbs);
-    if (elements > noalloc_scratch_words || lq > noalloc_scratch_words / elements)
+    if (lq > noalloc_scratch_words / elements)
     {
         return fail(HMPC_ERROR_INVALID_ARGUMENT, "batch too large for the allocation-free encryption");
     }

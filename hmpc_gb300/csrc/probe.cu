@@ -1,6 +1,11 @@
-#include "probe.hpp"
-
+// Rate probes of the benchmark: the integer-multiply throughput and the
+// ChaCha20 block rate of the device, the denominators of the integer-pipe and
+// integer-ALU rooflines (no vendor figure exists for 32-bit mad.lo / mad.hi or
+// for the keystream on this part).  Built into libhmpc_gb300_probes.so, a
+// measurement library beside the product library, not part of its C ABI.
 #include <cstdint>
+
+#include <cuda_runtime.h>
 
 #include "chacha.cuh"
 
@@ -182,4 +187,18 @@ namespace hmpc_gb300
         *ops_per_second = ops / (static_cast<double>(best) * 1e-3);
         return cudaSuccess;
     }
+}
+
+// 32-bit multiply operations (mad.lo and mad.hi each count one) per second on
+// the current device, timed on `stream`; 0 or the CUDA error code
+extern "C" int hmpc_bench_int_multiply_rate(void* stream, double* ops_per_second)
+{
+    return static_cast<int>(hmpc_gb300::probe_int_multiply_rate(static_cast<cudaStream_t>(stream), ops_per_second));
+}
+
+// ChaCha20 blocks per second (20 rounds, four output words used) on the
+// current device, timed on `stream`; 0 or the CUDA error code
+extern "C" int hmpc_bench_chacha_rate(void* stream, double* blocks_per_second)
+{
+    return static_cast<int>(hmpc_gb300::probe_chacha_rate(static_cast<cudaStream_t>(stream), blocks_per_second));
 }

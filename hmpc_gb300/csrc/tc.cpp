@@ -59,12 +59,6 @@ namespace
         return groups;
     }
 
-    // The carry of a group fed by digits takes two operations per digit while
-    // every column sum stays within (-2^22 + 2^15, 2^22 - 2^15); with digits
-    // |x| <= 128 that holds when each constant column's sum of |digit| is at
-    // most this bound (about twice what balanced random digits give)
-    constexpr uint32_t tc_byte_carry_column_bound = 32512;
-
     // the largest sum of |digit| over one column (output digit) of a group's images
     __global__ void tc_column_bound_kernel(const uint8_t* images, uint64_t columns, uint32_t n_mma,
                                            uint32_t image_bytes, uint32_t k_pad, uint32_t* out)
@@ -84,9 +78,11 @@ namespace
         atomicMax(out, static_cast<uint32_t>(sum));
     }
 
-    // whether a digit-fed group's constants keep its sums in the carry's range
-    int check_column_bound(hmpc_context* ctx, const TcGroupPlan& gp, const uint8_t* images, uint32_t* d_max,
-                           bool* fit)
+    // the largest column sum of |digit| of a digit-fed group's constants (the
+    // group keeps its sums in the two-operation carry's range while it is at
+    // most tc_byte_carry_column_bound)
+    int column_bound(hmpc_context* ctx, const TcGroupPlan& gp, const uint8_t* images, uint32_t* d_max,
+                     uint32_t* out)
     {
         const uint64_t columns = gp.blocks * gp.shape.splits * gp.shape.n_mma;
         HMPC_CUDA(cudaMemsetAsync(d_max, 0, sizeof(uint32_t), ctx->stream), "clearing the column bound");
@@ -97,7 +93,7 @@ namespace
         HMPC_CUDA(cudaMemcpyAsync(&bound, d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream),
                   "reading the column bound");
         HMPC_CUDA(cudaStreamSynchronize(ctx->stream), "checking tensor-core constants");
-        *fit = bound <= tc_byte_carry_column_bound;
+        *out = bound;
         return HMPC_OK;
     }
 
@@ -239,22 +235,24 @@ namespace
                 }
                 // the generation scratch is reused by the next group
                 cudaStreamSynchronize(ctx->stream);
-                bool fit = true;
                 if (gp.in_kind == tc_in_digits)
                 {
-                    if (int rc = check_column_bound(ctx, gp, tt.images + gp.offset, d_pow + pow256.size(), &fit))
+                    uint32_t bound = 0;
+                    if (int rc = column_bound(ctx, gp, tt.images + gp.offset, d_pow + pow256.size(), &bound))
                     {
                         cleanup();
                         cudaFree(tt.images);
                         return rc;
                     }
+                    tt.column_max = std::max(tt.column_max, bound);
                 }
-                if (!fit)
+                if (tt.column_max > ctx->tc_column_bound)
                 {
                     cleanup();
                     cudaFree(tt.images);
                     TcTables unfit;
                     unfit.fit = false;
+                    unfit.column_max = tt.column_max;
                     mod->tc_tables[key] = unfit;
                     return fail(HMPC_ERROR_UNSUPPORTED, "this modulus's tensor-core constants exceed the carry's "
                                                         "range; use a CUDA-core tile shape");
@@ -575,6 +573,32 @@ namespace hmpc_gb300::detail
             out->bytes += elements * (in + outb) + static_cast<double>(groups[j].blocks * shape.splits) * shape.b_bytes;
             out->flops += tiles * 2.0 * tc_rows * shape.n_mma * shape.k_pad;
         }
+        return HMPC_OK;
+    }
+
+    int tc_column_max(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, int splits, uint32_t* out)
+    {
+        if (!tc_supported(mod) || n < 16)
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core engine does not cover this transform");
+        }
+        if (splits != 1 && splits != 2)
+        {
+            return fail(HMPC_ERROR_INVALID_ARGUMENT, "the contiguous group splits 1 or 2 ways");
+        }
+        TcTables* tt = nullptr;
+        const int rc = prepare_tc(ctx, mod, n, inverse, splits, false, false, &tt);
+        if (rc && rc != HMPC_ERROR_UNSUPPORTED)
+        {
+            return rc;
+        }
+        std::lock_guard<std::mutex> lock(mod->tables_mutex);
+        auto it = mod->tc_tables.find(std::make_tuple(__builtin_ctzll(n), inverse ? 1 : 0, splits));
+        if (it == mod->tc_tables.end())
+        {
+            return rc ? rc : fail(HMPC_ERROR_CUDA, "tensor-core constants missing");
+        }
+        *out = it->second.column_max;
         return HMPC_OK;
     }
 

@@ -580,11 +580,19 @@ namespace hmpc_gb300
     }
 
     // the signed value sum_j x_j 2^(32 j) + top 2^(32 L), |value / q| < 2^15,
-    // reduced into [0, q)
+    // reduced into [0, q).  The quotient estimate reads the value's top word
+    // top * 2^32 + x[L-1] as one signed 64-bit integer converted once to f32
+    // (relative error 2^-24, so at most 2^-9 in the quotient), then scales by
+    // 2^(32(L-1)) / q; the dropped limbs add at most 1 / 32 for a top limb of
+    // q >= 32.  The estimate is within one of the quotient: one correction each
+    // way.  (Converting x[L-1] to f32 on its own would round a word near 2^32
+    // by up to 128 before a negative top cancels it -- 128 / 32 quotient units
+    // at the smallest top limb.)
     template<int L>
     __device__ __forceinline__ void tc_reduce(uint32_t (&x)[L], int top, const TcGroupParams& p)
     {
-        const float est = (static_cast<float>(top) * 4294967296.0f + static_cast<float>(x[L - 1])) * p.inv_q_top;
+        const long long top_word = static_cast<long long>(top) * 4294967296ll + static_cast<long long>(x[L - 1]);
+        const float est = static_cast<float>(top_word) * p.inv_q_top;
         const int t = __float2int_rd(est);
         long long carry = 0;
 #pragma unroll

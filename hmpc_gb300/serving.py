@@ -9,7 +9,7 @@ from dataclasses import dataclass, field
 
 from . import _lib, lhe
 from .comp import Tensor
-from .workloads import MODULI, chacha20_words
+from .moduli import MODULI, chacha20_words
 
 REQUEST_NTT, REQUEST_ENCRYPT, REQUEST_CT_MUL = 0, 1, 2
 QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, -2

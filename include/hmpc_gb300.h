@@ -65,15 +65,6 @@ int hmpc_context_set_nonce(hmpc_context* ctx, const uint32_t nonce[3]);
 /* Number of kernels launched through this context so far (no counterpart in
  * the reference; used to report launches per timed step). */
 int hmpc_context_launch_count(const hmpc_context* ctx, uint64_t* count);
-/* Measured 32-bit integer multiply throughput of the context's device in
- * operations per second (mad.lo and mad.hi each count one): the denominator of
- * the integer-pipe roofline.  No counterpart in the reference. */
-int hmpc_probe_int_multiply_rate(hmpc_context* ctx, double* ops_per_second);
-/* Measured ChaCha20 block rate of the context's device (20 rounds, one block
- * per (key, nonce, counter), four output words used, no memory traffic): the
- * denominator of the integer-ALU roofline of the fused samplers.  No
- * counterpart in the reference. */
-int hmpc_probe_chacha_rate(hmpc_context* ctx, double* blocks_per_second);
 /* hmpc::comp::queue::wait (hmpc/comp/queue.hpp:531-534) */
 int hmpc_context_synchronize(hmpc_context* ctx);
 
@@ -127,6 +118,20 @@ typedef struct hmpc_tc_cost
 } hmpc_tc_cost;
 int hmpc_modulus_tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int producer_kind, int splits,
                          hmpc_tc_cost* out);
+/* Exactness margin of the tensor-core engine (no counterpart in the
+ * reference).  A group fed by the digits of the group before it carries its
+ * column sums in two float operations per digit, exact while every sum stays
+ * below 2^22 - 2^15 in magnitude: with input digits of at most 128 in
+ * magnitude that holds when each column of the group's constant images has a
+ * sum of |digit| of at most 32512.  The engine checks this when it builds a
+ * modulus's constants for (n, direction, splits) and refuses the modulus for
+ * that transform if it fails (HMPC_ERROR_UNSUPPORTED; the CUDA-core tiles
+ * still run it).  hmpc_modulus_tc_column_max builds the constants if needed and
+ * reports their largest column sum; hmpc_context_set_tc_column_bound lowers
+ * the bound applied to constants built afterwards through this context
+ * (bound <= 32512), which lets a test drive the refusal. */
+int hmpc_modulus_tc_column_max(hmpc_modulus* mod, uint64_t n, int inverse, int splits, uint32_t* column_max);
+int hmpc_context_set_tc_column_bound(hmpc_context* ctx, uint32_t bound);
 /* Copy a cached twiddle table (n*L words, element-major) to host memory. */
 int hmpc_modulus_twiddles(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* host_table);
 
@@ -290,7 +295,10 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
  * 3*batch*n*L_q (+ batch*n*L_p for NTT-form plaintexts) must not exceed
  * 8 Mi words -- larger batches are rejected with HMPC_ERROR_INVALID_ARGUMENT.
  * The twiddle tables must already exist (hmpc_modulus_prepare) -- the call
- * refuses to build them.  The first call on a device looks up the array's
+ * refuses to build them.  Its transforms run on the CUDA-core tiles whatever
+ * plan q has (the tensor-core engine allocates digit buffers and constant
+ * images of its own), so it is slower than hmpc_lhe_enc where q's plan is the
+ * tensor-core engine; the ciphertexts are the same bits either way.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress); make that first call before any
  * stream capture.  All calls on a device share the array: calls that overlap
  * on the GPU (other streams, other contexts) race and must be serialised by

@@ -22,3 +22,13 @@ def test_last_error_without_device_calls():
     # argument validation happens before any CUDA call
     assert lib.hmpc_context_create(0, None, None, None) == 1
     assert b"null" in lib.hmpc_last_error()
+
+
+def test_rate_probe_library_is_separate():
+    """the benchmark's rate probes live in their own library, outside the
+    product's ABI"""
+    from hmpc_gb300 import build as _build
+
+    probes = ctypes.CDLL(str(_build.PROBES))
+    assert hasattr(probes, "hmpc_bench_int_multiply_rate") and hasattr(probes, "hmpc_bench_chacha_rate")
+    assert not any("probe" in name for name in _lib.declared_symbols())

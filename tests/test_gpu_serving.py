@@ -7,7 +7,7 @@ import pytest
 from hmpc_gb300 import lhe
 from hmpc_gb300.comp import Queue, Tensor
 from hmpc_gb300.serving import REQUEST_CT_MUL, REQUEST_ENCRYPT, REQUEST_NTT, Server, poisson_stream
-from hmpc_gb300.workloads import MODULI
+from hmpc_gb300.moduli import MODULI
 
 pytestmark = pytest.mark.gpu
 
@@ -94,6 +94,9 @@ def test_same_result_alone_and_in_the_mix(queue, oracle):
             om = oracle.Modulus(MODULI[a.q])
             a0, a1, b0, b1 = (t.numpy() for t in ins)
             assert np.array_equal(out[0], oracle.binary(om, oracle.OP_MUL, a0, b0))
+            cross = oracle.binary(om, oracle.OP_ADD, oracle.binary(om, oracle.OP_MUL, a0, b1),
+                                  oracle.binary(om, oracle.OP_MUL, a1, b0))
+            assert np.array_equal(out[1], cross)
             assert np.array_equal(out[2], oracle.binary(om, oracle.OP_MUL, a1, b1))
 
 

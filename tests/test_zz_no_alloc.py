@@ -83,3 +83,68 @@ def test_noalloc_rejects_oversized_batches_and_missing_tables(queue):
                                           c.ptr(), c.ptr())
     assert rc == 1
     assert b"hmpc_modulus_prepare" in _lib.load().hmpc_last_error()
+
+
+def test_noalloc_matches_the_oracle_and_a_tensor_core_plan(queue, oracle, cpu_threads):
+    """the allocation-free path (CUDA-core tiles, four transforms) against the
+    oracle directly, and against hmpc_lhe_enc with q's transforms on the
+    tensor-core engine (three stacked transforms): the same bits"""
+    n, batch = 1 << 11, 5
+    q, p = queue.modulus(Q_256), queue.modulus(P_64)
+    om_q, om_p = oracle.Modulus(Q_256), oracle.Modulus(P_64)
+    q.prepare(n)
+    p.prepare(n)
+    queue.nonce = [11, 0, 0]
+    key_a = queue.uniform(q, (), n)
+    key_b = queue.uniform(q, (), n)
+    msgs = queue.uniform(p, (batch,), n)
+    start = queue.nonce
+    got = encrypt(queue, "hmpc_lhe_enc_noalloc", q, p, n, batch, key_a, key_b, msgs, False)
+    c0, c1, _ = oracle.lhe_enc(om_q, om_p, n, batch, key_a.numpy(), key_b.numpy(), msgs.numpy(), False, KEY, start,
+                               threads=cpu_threads)
+    assert np.array_equal(got[0], c0) and np.array_equal(got[1], c1)
+    q.set_plan(n, batch, False, radix_bits=0)
+    queue.nonce = start
+    tc = encrypt(queue, "hmpc_lhe_enc", q, p, n, batch, key_a, key_b, msgs, False)
+    assert np.array_equal(tc[0], c0) and np.array_equal(tc[1], c1)
+    queue.nonce = start
+    again = encrypt(queue, "hmpc_lhe_enc_noalloc", q, p, n, batch, key_a, key_b, msgs, False)
+    assert np.array_equal(again[0], c0) and np.array_equal(again[1], c1)
+
+
+def test_noalloc_takes_no_device_memory(queue):
+    """On a fresh context whose tables are prepared, the first calls allocate
+    nothing: the device's free memory is the same before and after (the
+    library's fixed array is loaded by a call on another context first)."""
+    import torch
+
+    n, batch = 1 << 12, 6
+    q0, p0 = queue.modulus(Q_256), queue.modulus(P_64)
+    q0.prepare(n)
+    p0.prepare(n)
+    a0 = queue.uniform(q0, (), n)
+    m0 = queue.uniform(p0, (batch,), n)
+    encrypt(queue, "hmpc_lhe_enc_noalloc", q0, p0, n, batch, a0, a0, m0, False)
+    fresh = Queue(key=KEY)
+    q, p = fresh.modulus(Q_256), fresh.modulus(P_64)
+    q.prepare(n)
+    p.prepare(n)
+    key_a = fresh.uniform(q, (), n)
+    key_b = fresh.uniform(q, (), n)
+    msgs = fresh.uniform(p, (batch,), n)
+    c0, c1 = Tensor(q, (batch,), n), Tensor(q, (batch,), n)
+    fresh.wait()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        _lib.call("hmpc_lhe_enc_noalloc", fresh.handle, q.handle, p.handle, n, batch, key_a.ptr(), key_b.ptr(),
+                  msgs.ptr(), 0, c0.ptr(), c1.ptr())
+    fresh.wait()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+    # the regular entry point on the same context grows its workspace
+    _lib.call("hmpc_lhe_enc", fresh.handle, q.handle, p.handle, n, batch, key_a.ptr(), key_b.ptr(), msgs.ptr(), 0,
+              c0.ptr(), c1.ptr())
+    fresh.wait()
+    assert torch.cuda.mem_get_info()[0] < free_before
+    fresh.close()
