@@ -47,9 +47,11 @@ CONFIG = {
     "l2": "per-step working set 640 MiB (messages 64 MiB + ciphertexts 512 MiB + intermediates) > 129 MB L2",
 }
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
-# kernel: mean over the five tc_group_kernel launches of one fused CBD(10)
-# transform of 256 x 2^15 (one-pass ncu metrics captured at this size)
-DOMINANT_TRAFFIC_BYTES = 711.9e6
+# kernel: the mean over the five tc_group_kernel launches of one fused CBD(10)
+# transform of 256 x 2^15, from the one-pass ncu capture summarised in
+# profiles/tc_group_kernel_cbd_n32768_L8.md (sum of its five launches / 5)
+DOMINANT_TRAFFIC_BYTES = 628.0e6
+DOMINANT_TRAFFIC_PROFILE = "profiles/tc_group_kernel_cbd_n32768_L8.md"
 
 
 def rate_probes():
@@ -61,7 +63,9 @@ def rate_probes():
 
     import torch
 
-    from hmpc_gb300 import build as _build
+    import importlib
+
+    _build = importlib.import_module("hmpc_gb300.build")
 
     lib = ctypes.CDLL(str(_build.PROBES))
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -175,10 +179,11 @@ def run_reference(args, world, rank):
     oracle.build()
     threads = oracle.cpu_threads()
     q, p = oracle.Modulus(Q_256), oracle.Modulus(P_64)
-    # 32 encryptions per step: keygen is then about 3 % of a step, close to its
-    # 1/256 share of the GPU step, and the default 20 + 3 steps take about 20 s
-    # on 16 Arm cores
-    sample = max(1, int(os.environ.get("HMPC_REFERENCE_SAMPLE", "32")))
+    # keygen + 64 encryptions per step: keygen (two single-polynomial
+    # transforms and a uniform draw, about half an encryption) is then under
+    # 1 % of a step, against its 1/256 share of the GPU step; the driver's
+    # 20 + 5 steps take about 35 s on 16 Arm cores
+    sample = max(1, int(os.environ.get("HMPC_REFERENCE_SAMPLE", "64")))
 
     def step():
         s, a, b, nonce = oracle.lhe_keygen(q, p, N, SEED_KEY, [0, 0, 0], threads=threads)
@@ -215,6 +220,8 @@ def run_reference(args, world, rank):
             "kind": "port",
             "sample": f"keygen + {sample} encryptions per step at N=2^15, q 256-bit (the reference's SYCL build "
                       "needs a SYCL compiler and C++23, absent here; the oracle restates its algorithm)",
+            "keygen_amortised_over": sample,
+            "gpu_arm_keygen_amortised_over": BATCH,
         },
         "e2e": {"value": value, "unit": "encryptions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -236,6 +243,22 @@ def bf16_peak_tflops():
         return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"]), "measured"
     except (OSError, KeyError, ValueError):
         return 1900.0, "fallback"
+
+
+def algorithmic_8d(q, transform_ms, int_peak, hbm):
+    """The transform against the hot path's own work units, independent of
+    the engine: a negacyclic transform of degree N moves 2 * N * L * 4 bytes
+    per polynomial (read and write once, twiddles resident) and does
+    (N / 2) * log2(N) butterflies of one L-limb Montgomery product, 4L^2 + L
+    32-bit multiplies each.  The tensor-core engine does that work on the
+    tensor pipe, so the integer fraction can exceed 1."""
+    seconds = transform_ms * 1e-3
+    bytes_ = 2 * BATCH * N * q.limbs * 4
+    butterflies = BATCH * (N // 2) * (N.bit_length() - 1)
+    ops = butterflies * mont_mul_ops(q.limbs)
+    return {"bytes_per_transform": bytes_, "hbm_frac": bytes_ / seconds / 1e9 / hbm,
+            "butterflies_per_transform": butterflies, "int32_multiplies_per_transform": ops,
+            "int_frac": ops / seconds / int_peak, "transform_ms": transform_ms}
 
 
 def dominant_roofline(q, transform_ms, per_transform, int_peak, chacha_peak=None):
@@ -290,6 +313,9 @@ def dominant_roofline(q, transform_ms, per_transform, int_peak, chacha_peak=None
             "unit": primary["unit"],
             "frac": primary["frac"],
             "traffic": DOMINANT_TRAFFIC_BYTES,
+            "traffic_source": DOMINANT_TRAFFIC_PROFILE + " (ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                              "mean per launch)",
+            "algorithmic_8d": algorithmic_8d(q, transform_ms, int_peak, hbm),
             "peak_source": primary["peak_source"],
             "hbm_view" if bound == "tensor" else "tensor_view": other,
             "launches_per_transform": per_transform,
@@ -309,6 +335,7 @@ def dominant_roofline(q, transform_ms, per_transform, int_peak, chacha_peak=None
         "unit": "T int32-mul/s",
         "frac": achieved / int_peak,
         "traffic": None,
+        "algorithmic_8d": algorithmic_8d(q, transform_ms, int_peak, hbm),
         "peak_source": "measured live: hmpc_bench_int_multiply_rate (independent mad.lo/mad.hi chains)",
         "hbm_view": {"achieved": algorithmic_bytes / launch_s / 1e9, "peak": hbm, "unit": "GB/s",
                      "frac": algorithmic_bytes / launch_s / 1e9 / hbm, "peak_source": hbm_src},
@@ -767,6 +794,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-sustained", action="store_true",
+                    help="skip the one-second sustained loop (launch-list captures under a profiler)")
     ap.add_argument("--plan", default="tuned", choices=["tuned", "tensor"],
                     help="tensor: run q's batch transforms on the tensor-core engine (one constant image per "
                          "block, as the tuner picks on a GB300) instead of timing the candidates -- for captures "
@@ -835,6 +864,25 @@ def main():
     launches = queue.launches - launches0
     elapsed_ms = max_over_ranks(start.elapsed_time(stop), world, device="cuda")
     value = whole_job_rate(BATCH, world, args.steps, elapsed_ms)
+
+    # the same step in a loop of at least a second of device time, so that
+    # the clock sampler sees the GPU under sustained load (the K-step region
+    # above is the line's value)
+    sustained_steps = 0 if args.no_sustained else max(args.steps, int(1000.0 / max(elapsed_ms / args.steps, 1e-3)) + 1)
+    barrier()
+    s_start, s_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as s_clocks:
+        s_start.record(stream)
+        for _ in range(sustained_steps):
+            step(msgs)
+        s_stop.record(stream)
+        barrier()
+    sustained_ms = max_over_ranks(s_start.elapsed_time(s_stop), world, device="cuda")
+    sustained = None
+    if sustained_steps:
+        sustained = {"steps": sustained_steps, "device_s": sustained_ms * 1e-3,
+                     "value": whole_job_rate(BATCH, world, sustained_steps, sustained_ms),
+                     "ms_per_step": sustained_ms / sustained_steps, "clocks": s_clocks.summary()}
 
     # ------------------------------------- e2e through the API, host buffers
     # Every step copies its plaintexts in from pinned host memory, encrypts
@@ -955,6 +1003,7 @@ def main():
             "gpu_launches": launches,
             "roofline": roofline,
             "clocks": clocks.summary(),
+            "sustained": sustained,
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()

@@ -27,7 +27,9 @@ def test_last_error_without_device_calls():
 def test_rate_probe_library_is_separate():
     """the benchmark's rate probes live in their own library, outside the
     product's ABI"""
-    from hmpc_gb300 import build as _build
+    import importlib
+
+    _build = importlib.import_module("hmpc_gb300.build")
 
     probes = ctypes.CDLL(str(_build.PROBES))
     assert hasattr(probes, "hmpc_bench_int_multiply_rate") and hasattr(probes, "hmpc_bench_chacha_rate")
