@@ -112,6 +112,8 @@ SIGNATURES = {
                              ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_float)], _int),
     "hmpc_ntt_batch_status": ([_vp, ctypes.POINTER(ctypes.c_uint32)], _int),
     "hmpc_ntt_batch_destroy": ([_vp], _int),
+    "hmpc_ntt_batch_set_test_wait": ([_vp, ctypes.c_uint32, ctypes.c_uint32], _int),
+    "hmpc_context_set_test_wait": ([_vp, ctypes.c_uint32, _int], _int),
     "hmpc_cipher_enc": ([_vp, _u32p, _u32p, _u64, _int, _vp, _vp], _int),
     "hmpc_cipher_dec": ([_vp, _u32p, _u32p, _u64, _int, _vp, _vp], _int),
     "hmpc_fma": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp], _int),

@@ -670,6 +670,17 @@ int hmpc_modulus_tc_column_max(hmpc_modulus* mod, uint64_t n, int inverse, int s
     return tc_column_max(mod->ctx, mod, n, inverse != 0, splits, out);
 }
 
+int hmpc_context_set_test_wait(hmpc_context* ctx, uint32_t polls, int stall)
+{
+    if (!ctx)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null context");
+    }
+    ctx->tc_spin_limit = polls ? polls : tc_default_spin_limit;
+    ctx->tc_test_stall = stall ? 1u : 0u;
+    return HMPC_OK;
+}
+
 int hmpc_context_set_tc_column_bound(hmpc_context* ctx, uint32_t bound)
 {
     if (!ctx)

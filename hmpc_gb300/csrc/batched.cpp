@@ -34,6 +34,11 @@ struct hmpc_ntt_batch
     uint32_t items = 0;
     size_t smem = 0;
     unsigned grid = 0;
+    std::vector<uint32_t> item_wait_host, item_signal_host;
+    // polls of a wait before it gives up, and the test hook's withheld item
+    // (1-based, 0: none; hmpc_ntt_batch_set_test_wait)
+    uint32_t spin_limit = 1u << 24;  // ~1 s of 64 ns polls
+    uint32_t withheld = 0;
 
     // device state
     NttPassParams* d_params = nullptr;
@@ -176,6 +181,9 @@ struct hmpc_ntt_batch
             }
         }
         items = static_cast<uint32_t>(item_param.size());
+        item_wait_host = item_wait;
+        item_signal_host = item_signal;
+        withheld = 0;
         const size_t pbytes = params.size() * sizeof(NttPassParams);
         HMPC_CUDA(cudaMalloc(&d_params, pbytes), "allocating batch parameters");
         HMPC_CUDA(cudaMallocHost(&h_params, pbytes), "allocating batch parameters");
@@ -193,7 +201,17 @@ struct hmpc_ntt_batch
         HMPC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "querying SMs");
         const int per_sm = std::max(1, mod->kt->ntt_batched_blocks_per_sm(R, smem));
         grid = static_cast<unsigned>(std::min<uint64_t>(items, static_cast<uint64_t>(sms) * per_sm));
-        // graph: reset counters and control, then the persistent kernel
+        return capture();
+    }
+
+    // graph: reset counters and control, then the persistent kernel
+    int capture()
+    {
+        if (exec)
+        {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
         BatchedParams bp{};
         bp.params = d_params;
         bp.item_param = d_items;
@@ -204,13 +222,13 @@ struct hmpc_ntt_batch
         bp.counters = d_counters;
         bp.control = control();
         bp.items = items;
-        bp.spin_limit = 1u << 24;  // ~1 s of 64 ns polls
+        bp.spin_limit = spin_limit;
         cudaGraph_t graph = nullptr;
         HMPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capturing batch graph");
         cudaError_t e = cudaMemsetAsync(d_counters, 0, (degrees.size() + 4) * sizeof(uint32_t), stream);
         if (e == cudaSuccess)
         {
-            e = mod->kt->ntt_batched(bp, R, mod->h, grid, smem, stream);
+            e = mod->kt->ntt_batched(bp, radix_bits, mod->h, grid, smem, stream);
         }
         cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
         if (e != cudaSuccess || e2 != cudaSuccess)
@@ -228,6 +246,38 @@ struct hmpc_ntt_batch
             return cuda_fail(e, "instantiating batch graph");
         }
         return HMPC_OK;
+    }
+
+    // the test hook: item `item` (1-based, 0: none) waits for one signal more
+    // than its polynomial's earlier passes give, so its wait runs out after
+    // `polls` polls (0: the default limit)
+    int set_test_wait(uint32_t polls, uint32_t item)
+    {
+        if (item)
+        {
+            const uint32_t k = item - 1;
+            if (k >= items || item_signal_host[k] != 0 || item_wait_host[k] == 0)
+            {
+                return fail(HMPC_ERROR_INVALID_ARGUMENT,
+                            "the withheld item must be a work item of a polynomial's last pass after its first");
+            }
+        }
+        HMPC_CUDA(cudaStreamSynchronize(stream), "waiting for the batch");
+        auto put = [&](uint32_t k, uint32_t value) {
+            return cudaMemcpy(d_items + 2ull * items + k, &value, sizeof value, cudaMemcpyHostToDevice);
+        };
+        if (withheld)
+        {
+            HMPC_CUDA(put(withheld - 1, item_wait_host[withheld - 1]), "restoring the work list");
+            withheld = 0;
+        }
+        if (item)
+        {
+            HMPC_CUDA(put(item - 1, item_wait_host[item - 1] + 1u), "withholding a signal");
+            withheld = item;
+        }
+        spin_limit = polls ? polls : (1u << 24);
+        return capture();
     }
 
     int bind(const uint32_t* const* in, uint32_t* const* out)
@@ -487,6 +537,19 @@ int hmpc_ntt_batch_status(hmpc_ntt_batch* batch, uint32_t* failed_item)
         return fail(HMPC_ERROR_TIMEOUT, "a batched transform wait ran out; the outputs are incomplete");
     }
     return HMPC_OK;
+}
+
+int hmpc_ntt_batch_set_test_wait(hmpc_ntt_batch* batch, uint32_t polls, uint32_t withheld_item)
+{
+    if (!batch)
+    {
+        return fail(HMPC_ERROR_INVALID_ARGUMENT, "null batch");
+    }
+    if (int rc = enter(batch->ctx))
+    {
+        return rc;
+    }
+    return batch->set_test_wait(polls, withheld_item);
 }
 
 int hmpc_ntt_batch_destroy(hmpc_ntt_batch* batch)

@@ -63,6 +63,7 @@ namespace hmpc_gb300::detail
     // |x| <= 128 that holds when each constant column's sum of |digit| is at
     // most this bound (about twice what balanced random digits give)
     constexpr uint32_t tc_byte_carry_column_bound = 32512;
+    constexpr uint32_t tc_default_spin_limit = 1u << 20;
 
     // first group of a forward transform fed by x = p * CBD(V) + lift(m):
     // plaintext residues m mod p (nullptr: none) and the plaintext modulus
@@ -104,6 +105,11 @@ struct hmpc_context
     // this context (at most tc_byte_carry_column_bound; lowered only by tests
     // of the refusal)
     uint32_t tc_column_bound = hmpc_gb300::detail::tc_byte_carry_column_bound;
+    // polls of an mbarrier before a tensor-core group kernel gives up (each
+    // poll a try_wait that itself suspends for a bounded time), and the test
+    // hook that makes one such wait run out (hmpc_context_set_test_wait)
+    uint32_t tc_spin_limit = hmpc_gb300::detail::tc_default_spin_limit;
+    uint32_t tc_test_stall = 0;
     // a second stream for independent work of one call (fork / join events)
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t fork_event = nullptr;

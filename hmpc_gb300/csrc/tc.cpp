@@ -13,10 +13,6 @@ using namespace hmpc_gb300::detail;
 
 namespace
 {
-    // polls of an mbarrier before a group kernel reports HMPC_ERROR_TIMEOUT;
-    // each poll is a try_wait that itself suspends for a bounded time
-    constexpr uint32_t tc_spin_limit = 1u << 20;
-
     const TcKernels* kernels_of(const hmpc_modulus* mod)
     {
         return tc_kernels(mod->c.limbs);
@@ -384,7 +380,8 @@ namespace hmpc_gb300::detail
             p.tiles = gp.blocks * gp.shape.splits * p.tiles_per_block;
             p.log_n = log_n;
             p.lo = gp.lo;
-            p.spin_limit = tc_spin_limit;
+            p.spin_limit = ctx->tc_spin_limit;
+            p.test_stall = ctx->tc_test_stall;
             p.rng = ctx->rng();
             p.vx2 = vx2;
             p.nw = (2 * vx2 + 31) / 32;

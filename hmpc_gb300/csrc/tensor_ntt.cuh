@@ -86,6 +86,8 @@ namespace hmpc_gb300
         uint32_t log_n;
         uint32_t lo;               // column bits below the group's element bits
         uint32_t spin_limit;       // polls of an mbarrier before giving up
+        uint32_t test_stall;       // test hook: nonzero -- the MMA thread waits before its first tile on a
+                                   // barrier nothing arrives at, so that bounded wait runs out
         RngKey rng;                // CBD loader
         uint32_t vx2;
         uint32_t nw;
@@ -812,7 +814,8 @@ namespace hmpc_gb300
         uint64_t* bar_k0 = bars + 8;         // MMAs on the first K half complete (commit)
         uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 9);
         volatile uint32_t* abort_flag = tslot + 1;
-        static_assert(9 * sizeof(uint64_t) + 2 * sizeof(uint32_t) <= S::control_bytes, "control block");
+        uint64_t* bar_never = bars + 10;     // test hook: no thread arrives here
+        static_assert(11 * sizeof(uint64_t) <= S::control_bytes, "control block");
 
         const uint32_t tid = threadIdx.x;
         const uint32_t warp = tid >> 5, lane = tid & 31u;
@@ -846,6 +849,7 @@ namespace hmpc_gb300
             tc::mbar_init(&bar_acc_empty[0], tc_threads);
             tc::mbar_init(&bar_acc_empty[1], tc_threads);
             tc::mbar_init(bar_k0, 1);
+            tc::mbar_init(bar_never, 1);
             *abort_flag = 0;
             tc::mbar_init_fence();
         }
@@ -878,8 +882,12 @@ namespace hmpc_gb300
                 constexpr int ks_total = S::k_pad / 16;
                 constexpr int ks_half = NBUF == 1 ? (ks_total + 1) / 2 : ks_total;
                 constexpr uint32_t h0_bytes = NBUF == 1 ? 2u * ks_half * S::lbo_b : S::b_bytes;
+                // copies issued and waited for per barrier: on an abort the copies
+                // still in flight are waited for (bounded) before the CTA exits
+                uint32_t issued[2] = {0u, 0u}, landed[2] = {0u, 0u};
                 auto copy = [&](uint32_t jb, uint32_t piece) {
                     // NBUF 2: piece = buffer (whole image); NBUF 1: piece = K half
+                    ++issued[piece];
                     const uint8_t* src = p.images + (hb_first + jb) * S::b_bytes;
                     if constexpr (NBUF == 2)
                     {
@@ -940,6 +948,11 @@ namespace hmpc_gb300
                         give_up(4);
                         break;
                     }
+                    if (p.test_stall && i == 0 && !tc::mbar_wait(bar_never, 0u, p.spin_limit))
+                    {
+                        give_up(8);
+                        break;
+                    }
                     if (i >= 2 && !tc::mbar_wait(&bar_acc_empty[acc], static_cast<uint32_t>(((i - 2) >> 1) & 1u),
                                                  p.spin_limit))
                     {
@@ -948,10 +961,14 @@ namespace hmpc_gb300
                     }
                     const uint32_t piece0 = NBUF == 1 ? 0u : cur.jb % 2;
                     const uint32_t parity = NBUF == 1 ? (cur.jb & 1u) : ((cur.jb / 2) & 1u);
-                    if (new_block && !tc::mbar_wait(&bar_b[piece0], parity, p.spin_limit))
+                    if (new_block)
                     {
-                        give_up(1);
-                        break;
+                        if (!tc::mbar_wait(&bar_b[piece0], parity, p.spin_limit))
+                        {
+                            give_up(1);
+                            break;
+                        }
+                        ++landed[piece0];
                     }
                     tc::fence_after_sync();
                     const uint32_t a0 = tc::smem_u32(sa);
@@ -965,10 +982,14 @@ namespace hmpc_gb300
                     if constexpr (NBUF == 1)
                     {
                         tc::mma_commit(bar_k0);
-                        if (new_block && !tc::mbar_wait(&bar_b[1], parity, p.spin_limit))
+                        if (new_block)
                         {
-                            give_up(1);
-                            break;
+                            if (!tc::mbar_wait(&bar_b[1], parity, p.spin_limit))
+                            {
+                                give_up(1);
+                                break;
+                            }
+                            ++landed[1];
                         }
                         tc::fence_after_sync();
 #pragma unroll
@@ -983,6 +1004,19 @@ namespace hmpc_gb300
                     tc::mma_commit(bar_a_empty);
                     prev_jb = cur.jb;
                     cur = cur.next(tpb);
+                }
+                if (*abort_flag)
+                {
+                    // at most one copy per barrier is in flight (the next one into a
+                    // buffer is issued after the previous one was waited for): let
+                    // it land before the shared memory is released
+                    for (uint32_t piece = 0; piece < 2; ++piece)
+                    {
+                        if (issued[piece] > landed[piece])
+                        {
+                            tc::mbar_wait(&bar_b[piece], landed[piece] & 1u, p.spin_limit);
+                        }
+                    }
                 }
             }
         }

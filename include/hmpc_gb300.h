@@ -65,8 +65,20 @@ int hmpc_context_set_nonce(hmpc_context* ctx, const uint32_t nonce[3]);
 /* Number of kernels launched through this context so far (no counterpart in
  * the reference; used to report launches per timed step). */
 int hmpc_context_launch_count(const hmpc_context* ctx, uint64_t* count);
-/* hmpc::comp::queue::wait (hmpc/comp/queue.hpp:531-534) */
+/* hmpc::comp::queue::wait (hmpc/comp/queue.hpp:531-534).  Also reports
+ * HMPC_ERROR_TIMEOUT when a tensor-core transform launched since the last
+ * call gave up one of its bounded waits (and clears that state). */
 int hmpc_context_synchronize(hmpc_context* ctx);
+/* Test hook for the bounded waits of the tensor-core transform (no
+ * counterpart in the reference): every wait of its group kernels gives up
+ * after `polls` polls of an mbarrier (0: the default 2^20, each poll suspending
+ * for at most about a microsecond); with stall != 0 the thread that issues the
+ * MMAs of each launch first waits on a barrier that nothing arrives at, so
+ * that wait runs out: every launch returns early with its output incomplete,
+ * having waited for its copies in flight and freed its tensor memory, and
+ * hmpc_context_synchronize reports HMPC_ERROR_TIMEOUT.  stall = 0 restores
+ * normal operation; the context stays usable throughout. */
+int hmpc_context_set_test_wait(hmpc_context* ctx, uint32_t polls, int stall);
 
 /* --- moduli ---------------------------------------------------------------
  * mod<Q>'s compile-time constants (hmpc/ints/mod.hpp:90-127), computed at
@@ -200,6 +212,15 @@ int hmpc_ntt_batch_info(const hmpc_ntt_batch* batch, int* radix_bits, int* local
  * (HMPC_ERROR_TIMEOUT and the 1-based failing item when a bounded wait ran
  * out). */
 int hmpc_ntt_batch_status(hmpc_ntt_batch* batch, uint32_t* failed_item);
+/* Test hook for the bounded waits (no counterpart in the reference): a
+ * later-pass work item waits at most `polls` polls of about 64 ns (0: the
+ * default, about a second) for the earlier passes of its polynomial; with
+ * withheld_item != 0 that work item (1-based; it must belong to the last pass,
+ * after the first, of its polynomial) waits for one signal more than the
+ * earlier passes give, so its wait runs out: the run leaves that polynomial's
+ * output incomplete and hmpc_ntt_batch_status reports HMPC_ERROR_TIMEOUT with
+ * the item.  withheld_item = 0 restores the work list. */
+int hmpc_ntt_batch_set_test_wait(hmpc_ntt_batch* batch, uint32_t polls, uint32_t withheld_item);
 int hmpc_ntt_batch_destroy(hmpc_ntt_batch* batch);
 
 /* --- elementwise ----------------------------------------------------------- */
