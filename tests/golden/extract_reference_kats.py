@@ -268,8 +268,135 @@ def reduce_vectors(root):
     }
 
 
+def wire_vectors(root):
+    """hmpc's network message format as the reference states it: the
+    message-kind tags, type widths, feature bits and write order of
+    hmpc-rs/src/net.rs, the field list, byte diagrams, kind list and
+    datatype-tag examples of docs/networking.md, the message-id counter of
+    hmpc-rs/src/net/queue.rs and what the id hashes (hmpc-rs/src/net/metadata.rs)"""
+    out = {}
+    rel = "hmpc-rs/src/net.rs"
+    src = lines_of(root / rel)
+    kinds, in_enum = {}, False
+    for no, line in enumerate(src, 1):
+        if "pub enum MessageKind" in line:
+            in_enum = True
+        elif in_enum and line.strip() == "}":
+            in_enum = False
+        elif in_enum:
+            m = re.match(r"\s*(\w+) = (\d+),", line)
+            if m:
+                kinds[m.group(1)] = {"value": int(m.group(2)), "line": f"{rel}:{no}"}
+    out["kinds"] = kinds
+    types = {}
+    for no, line in enumerate(src, 1):
+        m = re.match(r"pub type (\w+) = u(\d+);", line)
+        if m:
+            types[m.group(1)] = {"bits": int(m.group(2)), "line": f"{rel}:{no}"}
+        m = re.match(r"const MESSAGE_FORMAT_VERSION: u8 = (\d+);", line)
+        if m:
+            out["version"] = {"value": int(m.group(1)), "line": f"{rel}:{no}"}
+        m = re.match(r"const SESSION_ID_SIZE: usize = (\d+) / 8;", line)
+        if m:
+            out["session_id_bytes"] = {"value": int(m.group(1)) // 8, "line": f"{rel}:{no}"}
+    out["types"] = types
+    flags, names = {}, {}
+    for no, line in enumerate(src, 1):
+        m = re.search(r'let (\w+) = cfg!\(feature = "(\w+)"\) as u8;', line)
+        if m:
+            names[m.group(1)] = m.group(2)
+        m = re.search(r"\| \((\w+) << (\d+)\)", line)
+        if m and m.group(1) in names:
+            flags[names[m.group(1)]] = {"bit": 1 << int(m.group(2)), "line": f"{rel}:{no}"}
+        elif re.match(r"\s*(\w+)$", line.strip()) and line.strip() in names:
+            flags[names[line.strip()]] = {"bit": 1, "line": f"{rel}:{no}"}
+    out["feature_flags"] = flags
+    order, in_write = [], False
+    for no, line in enumerate(src, 1):
+        if "async fn write_to(" in line:
+            in_write = True
+        elif in_write and "Ok(())" in line:
+            break
+        elif in_write:
+            m = re.search(r"stream\.write_all\(([\w.]+?)(?:\.to_le_bytes\(\)\.as_slice\(\))?\)\.await", line)
+            if m:
+                order.append({"field": m.group(1), "line": f"{rel}:{no}"})
+    out["write_order"] = order
+
+    rel = "docs/networking.md"
+    src = lines_of(root / rel)
+    fields = []
+    for no, line in enumerate(src, 1):
+        m = re.search(r"\[([\w ]+)\]\(#[\w-]+\) \((\d+) bit, `(\w)`\)", line)
+        if m:
+            fields.append({"name": m.group(1), "bits": int(m.group(2)), "symbol": m.group(3), "line": f"{rel}:{no}"})
+    out["doc_fields"] = fields
+    diagrams, title = {}, None
+    for no, line in enumerate(src, 1):
+        t = line.strip()
+        if t.endswith("enabled") and not t.startswith("-"):
+            title = t
+            diagrams[title] = {"rows": [], "line": f"{rel}:{no}"}
+            continue
+        m = re.match(r"\s*(\d+) \| ([a-z ]+) \|", line)
+        if m and title:
+            diagrams[title]["rows"].append({"bit_offset": int(m.group(1)), "symbols": m.group(2).split()})
+    out["diagrams"] = diagrams
+    doc_kinds = {}
+    for no, line in enumerate(src, 1):
+        m = re.match(r"- \[([\w ]+)\]\(#[\w-]+\) = (\d+)$", line.strip())
+        if m:
+            doc_kinds[m.group(1)] = {"value": int(m.group(2)), "line": f"{rel}:{no}"}
+        m = re.match(r"- Check consistency of \[([\w ]+)\]\(#[\w-]+\) = (\d+)$", line.strip())
+        if m:
+            doc_kinds["check " + m.group(1)] = {"value": int(m.group(2)), "line": f"{rel}:{no}"}
+    out["doc_kinds"] = doc_kinds
+    tags = []
+    for no, line in enumerate(src, 1):
+        m = re.search(r"`0x([0-9a-f]{2}) \| 0x([0-9a-f]{2}) = 0x([0-9a-f]{2})`", line)
+        if m:
+            tags.append({"bits": int(m.group(1), 16), "endianness": int(m.group(2), 16), "tag": int(m.group(3), 16),
+                         "line": f"{rel}:{no}"})
+    out["datatype_tags"] = tags
+
+    rel = "hmpc-rs/src/net/queue.rs"
+    src = lines_of(root / rel)
+    for no, line in enumerate(src, 1):
+        if ".or_insert(" in line:
+            out["counter_start"] = {"value": int(re.search(r"or_insert\((\d+)\)", line).group(1)),
+                                    "line": f"{rel}:{no}"}
+        if re.match(r"\s*id \+ counter\s*$", line):
+            out["id_plus_counter"] = {"line": f"{rel}:{no}"}
+        if "key.first_chunk::<MESSAGE_ID_SIZE>()" in line:
+            out["id_from_hash_prefix"] = {"line": f"{rel}:{no}"}
+
+    rel = "hmpc-rs/src/net/metadata.rs"
+    src = lines_of(root / rel)
+    hash_order, in_hash = [], False
+    members = {}
+    for no, line in enumerate(src, 1):
+        if re.search(r"fn hash\(&self, senders", line):
+            in_hash = True
+        elif in_hash and "sha.finish()" in line:
+            in_hash = False
+        elif in_hash:
+            m = re.search(r"(hash_communicator\((\w+)|hash_metadata)", line)
+            if m:
+                hash_order.append({"part": m.group(2) or "metadata", "line": f"{rel}:{no}"})
+        m = re.match(r"message!\((\w+)(?:, (\w+))?\);", line)
+        if m:
+            members[m.group(1)] = {"member": m.group(2), "line": f"{rel}:{no}"}
+        if "let len = communicator.len() as u64;" in line:
+            out["communicator_length"] = {"type": "u64", "line": f"{rel}:{no}"}
+    out["hash_order"] = hash_order
+    out["hash_members"] = members
+    return out
+
+
 def main():
-    root = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: extract_reference_kats.py /path/to/hmpc")
+    root = pathlib.Path(sys.argv[1])
     data = {
         "source": "hmpc v0.5.2 Catch2 tests, read as text",
         "chacha20": chacha_vectors(root),
@@ -280,6 +407,7 @@ def main():
         "linear_bgv": lhe_vectors(root),
         "matrix_vector_product": matvec_vectors(root),
         "reduce": reduce_vectors(root),
+        "wire": wire_vectors(root),
     }
     out = pathlib.Path(__file__).with_name("reference_kats.json")
     out.write_text(json.dumps(data, indent=1, default=str) + "\n")

@@ -109,3 +109,41 @@ def test_signing_feature_is_rejected(queue):
     with pytest.raises(_lib.HmpcError) as err:
         wire.pack(queue, [meta(0)], [t.data], wire.SIGNING)
     assert err.value.code == 2
+
+
+@pytest.mark.parametrize("mode,flags", [("no features enabled", 0), ("sessions feature enabled", wire.SESSIONS)])
+def test_device_headers_follow_the_documented_diagrams(queue, kats, mode, flags):
+    """the packed header bytes read back at the offsets of the reference's
+    own diagram (docs/networking.md "Visualizations", extracted into
+    tests/golden/reference_kats.json), field widths from its field list, kinds
+    and message ids from hmpc-rs (not from this repository's restatement)"""
+    from test_wire_cpu import documented_layout, reference_message_id
+
+    w = kats["wire"]
+    widths = {f["symbol"]: f["bits"] // 8 for f in w["doc_fields"]}
+    layout = documented_layout(kats, mode)
+    gq = queue.modulus(Q_256)
+    t = queue.uniform(gq, (2,), 64)
+    kinds = [("Broadcast", 7, 3), ("Gather", 4, 9), ("AllToAll", 65535, 2)]
+    metas = []
+    for i, (name, sender, receiver) in enumerate(kinds):
+        member = sender if name == "Broadcast" else receiver
+        mid = reference_message_id(kats, name, wire.U32, member, [sender, receiver], [sender, receiver],
+                                   w["counter_start"]["value"] + i)
+        metas.append({"kind": w["kinds"][name]["value"], "sender": sender, "receiver": receiver, "id": mid})
+    buf, offsets, sizes = wire.pack(queue, metas, [t.data] * len(metas), flags, SESSION if flags else None)
+    host = buf.cpu().numpy().tobytes()
+    payload = t.data.cpu().numpy().tobytes()
+    for m, off, size in zip(metas, offsets, sizes):
+        fields = {}
+        for offset, (sym, index) in layout.items():
+            fields.setdefault(sym, [0] * widths[sym])[index] = host[off + offset]
+        value = {sym: int.from_bytes(bytes(b), "little") for sym, b in fields.items()}
+        assert value["v"] == w["version"]["value"]
+        assert value["f"] == flags
+        assert (value["k"], value["t"], value["s"], value["r"], value["m"]) == \
+            (m["kind"], wire.U32, m["sender"], m["receiver"], m["id"])
+        if flags:
+            assert bytes(fields["i"]) == SESSION
+        header = max(layout) + 1
+        assert host[off + header:off + size] == payload
