@@ -451,6 +451,13 @@ def secondary_metrics(queue, int_peak):
     qb = queue.modulus(MODULI["q192"])
     xs = [queue.uniform(qb, (), n) for n in degrees]
     ys = [Tensor(qb, (), n) for n in degrees]
+    # the two engines on their own: the CUDA-core persistent kernel (default
+    # tile) and the tensor-core engine (one transform per degree, one graph)
+    engines = {}
+    for name, kw in (("cuda_core_default_tile", {"autotune": False}), ("tensor_core", {"tensor_cores": True})):
+        b = NttBatch(queue, qb, degrees, **kw)
+        engines[name] = {"ms": time_ms(lambda: b.run(xs, ys), 10), "tile": b.info()}
+        b.close()
     batch = NttBatch(queue, qb, degrees, autotune=True)
     ms_batch = time_ms(lambda: batch.run(xs, ys), 10)
     ms_calls = time_ms(lambda: [queue.ntt(xi, out=yi) for xi, yi in zip(xs, ys)], 3)
@@ -468,6 +475,7 @@ def secondary_metrics(queue, int_peak):
         "vs_tiled_per_polynomial_calls": ms_calls / ms_batch,
         "ms_plain_per_polynomial_calls": ms_plain,
         "tile": batch.info(),
+        "engines": engines,
     }
     batch.close()
     del xs, ys

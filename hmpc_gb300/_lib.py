@@ -22,6 +22,7 @@ ERRORS = {
 PRODUCER_TENSOR = 0
 PRODUCER_CBD = 1
 PRODUCER_UNIFORM = 2
+BATCH_DEFAULT, BATCH_AUTOTUNE, BATCH_TENSOR_CORES = 0, 1, 2
 OP_ADD, OP_SUB, OP_MUL = 0, 1, 2
 REDUCE_OPS = {"add": 0, "multiply": 1, "bit_and": 2, "bit_or": 3, "bit_xor": 4, "min": 5, "max": 6}
 

@@ -11,14 +11,18 @@ from .comp import Tensor
 class NttBatch:
     """A planned batch: `degrees[i]` is the ring degree of polynomial i."""
 
-    def __init__(self, queue, modulus, degrees, inverse=False, autotune=True):
+    def __init__(self, queue, modulus, degrees, inverse=False, autotune=True, tensor_cores=False):
+        """autotune: time the CUDA-core tile shapes and the tensor-core engine
+        and keep the fastest; tensor_cores: the tensor-core engine (one
+        transform per degree over the polynomials' own buffers)"""
         self.queue = queue
         self.modulus = modulus
         self.degrees = [int(d) for d in degrees]
         handle = ctypes.c_void_p()
         arr = (ctypes.c_uint64 * len(self.degrees))(*self.degrees)
+        mode = _lib.BATCH_TENSOR_CORES if tensor_cores else (_lib.BATCH_AUTOTUNE if autotune else _lib.BATCH_DEFAULT)
         _lib.call("hmpc_ntt_batch_create", queue.handle, modulus.handle, len(self.degrees), arr, int(inverse),
-                  int(autotune), ctypes.byref(handle))
+                  mode, ctypes.byref(handle))
         self.handle = handle
 
     def info(self):
@@ -26,8 +30,8 @@ class NttBatch:
         items, ms = ctypes.c_uint32(), ctypes.c_float()
         _lib.call("hmpc_ntt_batch_info", self.handle, ctypes.byref(r), ctypes.byref(lb), ctypes.byref(cb),
                   ctypes.byref(items), ctypes.byref(ms))
-        return {"radix": 1 << r.value, "local_bits": lb.value, "col_bits": cb.value, "items": items.value,
-                "tuned_ms": ms.value}
+        return {"engine": "tensor" if r.value == 0 else "cuda", "radix": 1 << r.value, "local_bits": lb.value,
+                "col_bits": cb.value, "items": items.value, "tuned_ms": ms.value}
 
     def run(self, inputs, outputs=None):
         """inputs / outputs: lists of Tensors (one polynomial each)"""

@@ -18,7 +18,7 @@ LIB = OUT / "libhmpc_gb300.so"
 PROBES = OUT / "libhmpc_gb300_probes.so"
 INCLUDE = HERE.parent / "include"
 LIMBS = range(1, 10)
-TC_LIMBS = (2, 4, 8)  # limb counts of the tensor-core transform
+TC_LIMBS = range(2, 9)  # limb counts of the tensor-core transform
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -714,7 +714,7 @@ int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inv
         }
         if (!tc_supported(mod))
         {
-            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core transform needs a 2-, 4- or 8-limb modulus below "
+            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core transform needs a 2- to 8-limb modulus below "
                                                 "0.996 * 2^(32L) whose top limb is at least 32");
         }
     }

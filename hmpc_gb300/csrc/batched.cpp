@@ -51,6 +51,22 @@ struct hmpc_ntt_batch
     std::vector<const uint32_t*> bound_in;
     std::vector<uint32_t*> bound_out;
 
+    // tensor-core engine (radix_bits 0): the polynomials bucketed by degree,
+    // each bucket one transform whose first group reads and last group writes
+    // the polynomials' own buffers through device pointer tables
+    struct Bucket
+    {
+        uint64_t n = 0;
+        std::vector<uint32_t> polys;
+        size_t table = 0;  // offset of its in-pointers in the tables (out-pointers follow)
+    };
+    bool tc = false;
+    std::vector<Bucket> buckets;
+    void** d_tables = nullptr;  // device pointer tables
+    void** h_tables = nullptr;  // pinned staging
+    size_t table_entries = 0;
+    uint32_t* d_digits = nullptr;
+
     void release_plan()
     {
         if (exec)
@@ -62,10 +78,19 @@ struct hmpc_ntt_batch
         cudaFree(d_items);
         cudaFree(d_counters);
         cudaFreeHost(h_params);
+        cudaFree(d_tables);
+        cudaFreeHost(h_tables);
+        cudaFree(d_digits);
         d_params = nullptr;
         d_items = nullptr;
         d_counters = nullptr;
         h_params = nullptr;
+        d_tables = nullptr;
+        h_tables = nullptr;
+        d_digits = nullptr;
+        table_entries = 0;
+        tc = false;
+        buckets.clear();
         bound_in.clear();
         bound_out.clear();
     }
@@ -94,6 +119,111 @@ struct hmpc_ntt_batch
     BatchedControl* control() const
     {
         return reinterpret_cast<BatchedControl*>(d_counters + degrees.size());
+    }
+
+    // whether the tensor-core engine covers every polynomial of the batch
+    bool tc_covers() const
+    {
+        if (!tc_supported(mod))
+        {
+            return false;
+        }
+        for (uint64_t n : degrees)
+        {
+            if (n < 16)
+            {
+                return false;
+            }
+        }
+        return true;
+    }
+
+    // The tensor-core configuration: buckets by degree (largest first), the
+    // constants and launch state of each degree built now, then one graph of
+    // every bucket's group launches on the batch stream.
+    int build_tc(int splits)
+    {
+        release_plan();
+        tc = true;
+        radix_bits = 0;
+        local_bits = splits;
+        col_bits = 0;
+        std::vector<uint64_t> sizes(degrees.begin(), degrees.end());
+        std::sort(sizes.begin(), sizes.end(), std::greater<uint64_t>());
+        sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+        uint64_t digit_words = 0;
+        for (uint64_t n : sizes)
+        {
+            Bucket bk;
+            bk.n = n;
+            for (size_t i = 0; i < degrees.size(); ++i)
+            {
+                if (degrees[i] == n)
+                {
+                    bk.polys.push_back(static_cast<uint32_t>(i));
+                }
+            }
+            bk.table = table_entries;
+            table_entries += 2 * bk.polys.size();
+            uint64_t per_element = 0;
+            if (int rc = tc_prepare_polys(ctx, mod, n, inverse, splits, &per_element))
+            {
+                return rc;
+            }
+            digit_words = std::max<uint64_t>(digit_words, per_element * n * bk.polys.size());
+            buckets.push_back(std::move(bk));
+        }
+        HMPC_CUDA(cudaMalloc(&d_tables, table_entries * sizeof(void*)), "allocating pointer tables");
+        HMPC_CUDA(cudaMallocHost(&h_tables, table_entries * sizeof(void*)), "allocating pointer tables");
+        std::memset(h_tables, 0, table_entries * sizeof(void*));
+        if (digit_words)
+        {
+            HMPC_CUDA(cudaMalloc(&d_digits, digit_words * sizeof(uint32_t)), "allocating digit buffers");
+        }
+        return capture_tc();
+    }
+
+    int capture_tc()
+    {
+        if (exec)
+        {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+        // the captured launches are counted per replay, not here
+        const uint64_t launches_before = ctx->launches;
+        cudaGraph_t graph = nullptr;
+        HMPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capturing batch graph");
+        int rc = HMPC_OK;
+        for (const Bucket& bk : buckets)
+        {
+            auto** table = d_tables + bk.table;
+            rc = run_tc_polys(ctx, mod, bk.n, bk.polys.size(), inverse, local_bits,
+                              reinterpret_cast<const uint32_t* const*>(table),
+                              reinterpret_cast<uint32_t* const*>(table + bk.polys.size()), d_digits, stream);
+            if (rc)
+            {
+                break;
+            }
+        }
+        items = static_cast<uint32_t>(ctx->launches - launches_before);
+        ctx->launches = launches_before;
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (rc || e != cudaSuccess)
+        {
+            if (graph)
+            {
+                cudaGraphDestroy(graph);
+            }
+            return rc ? rc : cuda_fail(e, "capturing batch graph");
+        }
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess)
+        {
+            return cuda_fail(e, "instantiating batch graph");
+        }
+        return HMPC_OK;
     }
 
     // Build the work list and device arrays for one configuration.
@@ -253,6 +383,10 @@ struct hmpc_ntt_batch
     // `polls` polls (0: the default limit)
     int set_test_wait(uint32_t polls, uint32_t item)
     {
+        if (tc)
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core batch's waits follow hmpc_context_set_test_wait");
+        }
         if (item)
         {
             const uint32_t k = item - 1;
@@ -293,6 +427,31 @@ struct hmpc_ntt_batch
         }
         // the staging buffer may still feed the previous copy
         HMPC_CUDA(cudaStreamSynchronize(stream), "waiting for the previous batch");
+        if (tc)
+        {
+            for (size_t i = 0; i < degrees.size(); ++i)
+            {
+                if ((reinterpret_cast<uintptr_t>(in[i]) | reinterpret_cast<uintptr_t>(out[i])) & 15u)
+                {
+                    return fail(HMPC_ERROR_INVALID_ARGUMENT,
+                                "the tensor-core batch needs 16-byte aligned polynomial buffers");
+                }
+            }
+            for (const Bucket& bk : buckets)
+            {
+                for (size_t k = 0; k < bk.polys.size(); ++k)
+                {
+                    h_tables[bk.table + k] = const_cast<uint32_t*>(in[bk.polys[k]]);
+                    h_tables[bk.table + bk.polys.size() + k] = out[bk.polys[k]];
+                }
+            }
+            HMPC_CUDA(cudaMemcpyAsync(d_tables, h_tables, table_entries * sizeof(void*), cudaMemcpyHostToDevice,
+                                      stream),
+                      "uploading batch pointers");
+            bound_in.assign(in, in + degrees.size());
+            bound_out.assign(out, out + degrees.size());
+            return HMPC_OK;
+        }
         for (size_t k = 0; k < params.size(); ++k)
         {
             const uint32_t i = param_poly[k];
@@ -318,7 +477,7 @@ struct hmpc_ntt_batch
         HMPC_CUDA(cudaGraphLaunch(exec, stream), "launching batch graph");
         HMPC_CUDA(cudaEventRecord(finish, stream), "ordering batch");
         HMPC_CUDA(cudaStreamWaitEvent(ctx->stream, finish, 0), "ordering batch");
-        ++ctx->launches;
+        ctx->launches += tc ? items : 1;
         return HMPC_OK;
     }
 };
@@ -405,7 +564,17 @@ int hmpc_ntt_batch_create(hmpc_context* ctx, hmpc_modulus* mod, uint64_t count, 
     PlanOptions def;
     const int b_default = local_bits_for(L, def);
     int best_r = 3, best_b = b_default, best_c = 4;
-    if (autotune)
+    if (autotune == HMPC_BATCH_TENSOR_CORES)
+    {
+        if (!b->tc_covers())
+        {
+            delete b;
+            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core engine does not cover this modulus or a degree below 16");
+        }
+        best_r = 0;
+        best_b = 1;
+    }
+    else if (autotune)
     {
         // scratch buffers for the trial runs
         std::vector<uint32_t*> bufs;
@@ -451,6 +620,22 @@ int hmpc_ntt_batch_create(hmpc_context* ctx, hmpc_modulus* mod, uint64_t count, 
                     }
                 }
             }
+            // the tensor-core engine, one bucket per degree, with either split
+            // of the groups whose rows are contiguous elements
+            for (int splits : {1, 2})
+            {
+                if (!b->tc_covers() || b->build_tc(splits) != HMPC_OK)
+                {
+                    break;
+                }
+                const float ms = time_config(b, ins, bufs);
+                if (ms < best)
+                {
+                    best = ms;
+                    best_r = 0;
+                    best_b = splits;
+                }
+            }
         }
         cudaStreamSynchronize(b->stream);
         for (auto* p : bufs)
@@ -459,7 +644,7 @@ int hmpc_ntt_batch_create(hmpc_context* ctx, hmpc_modulus* mod, uint64_t count, 
         }
         b->tuned_ms = best < 1e29f ? best : 0.f;
     }
-    if (int rc = b->build(best_r, best_b, best_c))
+    if (int rc = best_r == 0 ? b->build_tc(best_b) : b->build(best_r, best_b, best_c))
     {
         delete b;
         return rc;
@@ -528,8 +713,26 @@ int hmpc_ntt_batch_status(hmpc_ntt_batch* batch, uint32_t* failed_item)
     {
         return rc;
     }
-    BatchedControl control{};
     HMPC_CUDA(cudaStreamSynchronize(batch->stream), "waiting for the batch");
+    if (batch->tc)
+    {
+        // the tensor-core groups report a wait that ran out in the context's error word
+        *failed_item = 0;
+        hmpc_context* ctx = batch->ctx;
+        if (ctx->tc_error)
+        {
+            uint32_t code = 0;
+            HMPC_CUDA(cudaMemcpy(&code, ctx->tc_error, sizeof code, cudaMemcpyDeviceToHost), "reading batch status");
+            if (code)
+            {
+                HMPC_CUDA(cudaMemset(ctx->tc_error, 0, sizeof code), "clearing the error word");
+                return fail(HMPC_ERROR_TIMEOUT, "a tensor-core group of the batch gave up a wait; the outputs are "
+                                                "incomplete");
+            }
+        }
+        return HMPC_OK;
+    }
+    BatchedControl control{};
     HMPC_CUDA(cudaMemcpy(&control, batch->control(), sizeof control, cudaMemcpyDeviceToHost), "reading batch status");
     *failed_item = control.error;
     if (control.error || control.done != batch->items)

@@ -100,8 +100,8 @@ namespace hmpc_gb300
         uint32_t splits = 1;  // constant images per block (output elements split over them)
     };
 
-    // tensor-core transform kernels of one limb count (2, 4 or 8 limbs: 8, 16 or
-    // 32 digits per residue)
+    // tensor-core transform kernels of one limb count (2 to 8 limbs: 4L digits
+    // per residue)
     struct TcKernels
     {
         int digits;
@@ -114,7 +114,11 @@ namespace hmpc_gb300
     };
 
     const TcKernels* tc_kernels_2();
+    const TcKernels* tc_kernels_3();
     const TcKernels* tc_kernels_4();
+    const TcKernels* tc_kernels_5();
+    const TcKernels* tc_kernels_6();
+    const TcKernels* tc_kernels_7();
     const TcKernels* tc_kernels_8();
 
     inline const TcKernels* tc_kernels(int limbs)
@@ -122,7 +126,11 @@ namespace hmpc_gb300
         switch (limbs)
         {
         case 2: return tc_kernels_2();
+        case 3: return tc_kernels_3();
         case 4: return tc_kernels_4();
+        case 5: return tc_kernels_5();
+        case 6: return tc_kernels_6();
+        case 7: return tc_kernels_7();
         case 8: return tc_kernels_8();
         default: return nullptr;
         }

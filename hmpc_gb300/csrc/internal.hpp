@@ -268,7 +268,7 @@ namespace hmpc_gb300::detail
     int run_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
                   uint32_t vx2, uint32_t security, const uint32_t* src, uint32_t* out);
     CastParams make_cast(const hmpc_modulus* dst, const hmpc_modulus* src);
-    // tensor-core engine: whether the modulus qualifies (2, 4 or 8 limbs, q
+    // tensor-core engine: whether the modulus qualifies (2 to 8 limbs, q
     // below 0.996 * 2^(32L), top limb at least 32) and whether a call does
     // (forward from a tensor or CBD(V) samples, or inverse; at least 16
     // coefficients; no per-polynomial RNG)
@@ -294,6 +294,18 @@ namespace hmpc_gb300::detail
     int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
                        int count, uint32_t* out, int splits);
     int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out);
+    // Polynomials of one degree n in buffers of their own (the batched
+    // transform's buckets).  tc_prepare_polys builds the constants of (n,
+    // direction, splits) and the launch state outside any stream capture and
+    // gives the digit words per element the transform needs in `digits`;
+    // run_tc_polys launches the groups on `stream` (capturable): the first
+    // group reads in_polys[i], the last writes out_polys[i] (device pointer
+    // tables of `count` entries, buffers 16-byte aligned).
+    int tc_prepare_polys(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, int splits,
+                         uint64_t* digit_words_per_element);
+    int run_tc_polys(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t count, bool inverse, int splits,
+                     const uint32_t* const* in_polys, uint32_t* const* out_polys, uint32_t* digits,
+                     cudaStream_t stream);
     // builds (once) the constants of the transform (n, direction, splits) and
     // reports their largest column sum of |digit|
     int tc_column_max(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, int splits, uint32_t* out);

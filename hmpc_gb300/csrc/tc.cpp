@@ -336,10 +336,16 @@ namespace hmpc_gb300::detail
         TcTables* tt;
         uint32_t log_n;
         float inv_q_top;
+        cudaStream_t stream = nullptr;
+        // polynomials in buffers of their own: the first group's input and
+        // the last group's output tables (device arrays of pointers)
+        const uint32_t* const* in_polys = nullptr;
+        uint32_t* const* out_polys = nullptr;
 
         int init(hmpc_context* c, hmpc_modulus* m, uint64_t n, TcTables* t)
         {
             ctx = c;
+            stream = c->stream;
             mod = m;
             k = kernels_of(m);
             tt = t;
@@ -407,7 +413,15 @@ namespace hmpc_gb300::detail
             const unsigned grid =
                 static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
             const int splits = first_sampled ? 1 : static_cast<int>(gp.shape.splits);
-            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, gp.layout, grid, ctx->stream);
+            if (j == 0)
+            {
+                p.in_polys = in_polys;
+            }
+            if (j + 1 == tt->groups.size())
+            {
+                p.out_polys = out_polys;
+            }
+            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, gp.layout, grid, stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching a tensor-core transform group");
@@ -532,6 +546,65 @@ namespace hmpc_gb300::detail
             const uint32_t* in = digits + (((j - 1) & 1u) ? w * total : 0);
             uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * total : 0);
             if (int rc = run.group(j, in, o, total, batch * static_cast<uint64_t>(count), tc_in_digits, 0, nullptr, 0))
+            {
+                return rc;
+            }
+        }
+        return HMPC_OK;
+    }
+
+    int tc_prepare_polys(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, bool inverse, int splits,
+                         uint64_t* digit_words_per_element)
+    {
+        if (!tc_supported(mod) || n < 16 || (splits != 1 && splits != 2))
+        {
+            return fail(HMPC_ERROR_UNSUPPORTED, "the tensor-core engine does not cover this transform");
+        }
+        TcTables* tt = nullptr;
+        if (int rc = prepare_tc(ctx, mod, n, inverse, splits, false, false, &tt))
+        {
+            return rc;
+        }
+        TcLaunch run;
+        if (int rc = run.init(ctx, mod, n, tt))
+        {
+            return rc;
+        }
+        const uint64_t w = tt->groups.front().shape.w_out;
+        *digit_words_per_element = tt->groups.size() > 1 ? (tt->groups.size() > 2 ? 2 : 1) * w : 0;
+        return HMPC_OK;
+    }
+
+    int run_tc_polys(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t count, bool inverse, int splits,
+                     const uint32_t* const* in_polys, uint32_t* const* out_polys, uint32_t* digits,
+                     cudaStream_t stream)
+    {
+        TcTables* tt = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(mod->tables_mutex);
+            auto it = mod->tc_tables.find(std::make_tuple(__builtin_ctzll(n), inverse ? 1 : 0, splits));
+            if (it == mod->tc_tables.end() || !it->second.fit || !it->second.images)
+            {
+                return fail(HMPC_ERROR_INVALID_ARGUMENT, "tensor-core constants not prepared for this degree");
+            }
+            tt = &it->second;
+        }
+        const uint64_t elements = n * count;
+        const uint64_t w = tt->groups.front().shape.w_out;
+        const size_t stages = tt->groups.size();
+        TcLaunch run;
+        if (int rc = run.init(ctx, mod, n, tt))
+        {
+            return rc;
+        }
+        run.stream = stream;
+        run.in_polys = in_polys;
+        run.out_polys = out_polys;
+        for (size_t j = 0; j < stages; ++j)
+        {
+            const uint32_t* in = j == 0 ? nullptr : digits + (((j - 1) & 1u) ? w * elements : 0);
+            uint32_t* o = j + 1 == stages ? nullptr : digits + ((j & 1u) ? w * elements : 0);
+            if (int rc = run.group(j, in, o, elements, count, j == 0 ? tc_in_limbs : tc_in_digits, 0, nullptr, 0))
             {
                 return rc;
             }

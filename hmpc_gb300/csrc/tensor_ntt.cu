@@ -1,5 +1,5 @@
 // Tensor-core transform kernels of one limb count, compiled with
-// -DHMPC_L=<2|4|8>; exports tc_kernels_<L>().  Instantiated group shapes:
+// -DHMPC_L=<2..8>; exports tc_kernels_<L>().  Instantiated group shapes:
 // the first group (r = 8) from limbs or from centred binomial samples, the
 // middle groups (r = 8) digits to digits, the last group (r = 2, 4 or 8)
 // digits to reduced limbs.
@@ -21,7 +21,7 @@ namespace hmpc_gb300
     {
         constexpr int L = HMPC_L;
         constexpr int DC = 4 * L;
-        static_assert(L == 2 || L == 4 || L == 8, "tensor-core transform for 2, 4 or 8 limbs");
+        static_assert(L >= 2 && L <= 8, "tensor-core transform for 2 to 8 limbs");
 
         Modulus<L> device_modulus(const HostModulus& h)
         {

@@ -102,6 +102,12 @@ namespace hmpc_gb300
         uint32_t pq[2];
         uint32_t pninv;
         uint32_t phalf[2];
+        // polynomials in buffers of their own (limb-planar, N words per plane,
+        // 16-byte aligned): the first group reads in_polys[i] instead of `in`
+        // and the last group writes out_polys[i] instead of `out` (nullptr: the
+        // batch is one buffer of `elements` words per plane)
+        const uint32_t* const* in_polys;
+        uint32_t* const* out_polys;
     };
 
     // base-256 digits of the small-integer input (|x| < 2^70 for p < 2^64, 2V <= 64):
@@ -240,13 +246,20 @@ namespace hmpc_gb300
             const uint32_t row = tid % tc_rows, part = tid / tc_rows;
             const TcRow r = tc_row<S::g>(p, h, mt, row);
             const uint32_t* rp = p.in + r.base;
+            uint64_t stride = p.elements;
+            if (p.in_polys)
+            {
+                // the row's polynomial in its own buffer (read only for rows in range)
+                stride = 1ull << p.log_n;
+                rp = r.ok ? p.in_polys[r.poly] + (r.base & (stride - 1ull)) : p.in;
+            }
             const bool contiguous = p.lo == 0;  // the row's R elements are adjacent: vector loads
 #pragma unroll
             for (int wi = 0; wi < wh; ++wi)
             {
                 const uint32_t w = part + tc_parts * wi;
                 const bool live = r.ok && w < static_cast<uint32_t>(S::w_in);
-                const uint32_t* wp = InBlk ? p.in + r.base * S::w_in + w * R : rp + w * p.elements;
+                const uint32_t* wp = InBlk ? p.in + r.base * S::w_in + w * R : rp + w * stride;
                 if (live && contiguous)
                 {
                     if constexpr (R == 8)
@@ -574,11 +587,33 @@ namespace hmpc_gb300
         }
     };
 
+    // the DC column sums of one output element: one TMEM load of 32, or
+    // loads of 16, 8 and 4 consecutive columns that add up to DC (digit counts
+    // of 2..8 limbs), completed by one wait
     template<int DC>
     __device__ __forceinline__ void tc_load_sums(uint32_t taddr, uint32_t (&s)[DC])
     {
-        static_assert(DC == 8 || DC == 16 || DC == 32, "digit counts of 2, 4 and 8 limbs");
-        tc::tmem_load<DC>(taddr, s);
+        static_assert(DC % 4 == 0 && DC >= 8 && DC <= 32, "digit counts of 2 to 8 limbs");
+        if constexpr (DC == 32)
+        {
+            tc::tmem_load<32>(taddr, s);
+        }
+        else
+        {
+            constexpr int a16 = DC & 16, a8 = DC & 8, a4 = DC & 4;
+            if constexpr (a16 != 0)
+            {
+                tc::tmem_load<16>(taddr, *reinterpret_cast<uint32_t(*)[16]>(&s[0]));
+            }
+            if constexpr (a8 != 0)
+            {
+                tc::tmem_load<8>(taddr + a16, *reinterpret_cast<uint32_t(*)[8]>(&s[a16]));
+            }
+            if constexpr (a4 != 0)
+            {
+                tc::tmem_load<4>(taddr + a16 + a8, *reinterpret_cast<uint32_t(*)[4]>(&s[a16 + a8]));
+            }
+        }
     }
 
     // the signed value sum_j x_j 2^(32 j) + top 2^(32 L), |value / q| < 2^15,
@@ -688,6 +723,12 @@ namespace hmpc_gb300
         const uint32_t kl0 = (warp >> 2) * per;      // first local output of this thread
         const uint32_t k0 = split * outputs + kl0;   // its element index in the group
         uint32_t* op = p.out + r.base;
+        uint64_t ostride = p.elements;
+        if (p.out_polys)
+        {
+            ostride = 1ull << p.log_n;
+            op = r.ok ? p.out_polys[r.poly] + (r.base & (ostride - 1ull)) : p.out;
+        }
         uint32_t res[Contig ? words_out : 1][Contig ? per : 1];
 #pragma unroll
         for (int kk = 0; kk < per; ++kk)
@@ -761,7 +802,7 @@ namespace hmpc_gb300
 #pragma unroll
                     for (int w = 0; w < words_out; ++w)
                     {
-                        op[w * p.elements + e] = words[w];
+                        op[w * ostride + e] = words[w];
                     }
                 }
             }
@@ -773,7 +814,7 @@ namespace hmpc_gb300
 #pragma unroll
                 for (int w = 0; w < words_out; ++w)
                 {
-                    store_run<per>(op + w * p.elements + k0, res[w]);
+                    store_run<per>(op + w * ostride + k0, res[w]);
                 }
             }
         }

@@ -101,7 +101,7 @@ int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root
  * direction: register radix bits (2 or 3: 4 or 8 elements per thread), tile
  * bits (log2 elements a CTA stages; 0 = by shared-memory budget) and column
  * bits (coalescing width) -- or radix bits 0: the tensor-core engine (exact
- * fp16 MMAs over 8-bit digits, 2-, 4- and 8-limb moduli below
+ * fp16 MMAs over 8-bit digits, moduli of 2 to 8 limbs below
  * 0.996 * 2^(32L); tensor and CBD(V) producers; other calls of that shape
  * run the default tiles), whose local_bits selects the output split (1 or 2,
  * 0 = 1) of the group with contiguous rows.  No counterpart in the reference (its transform
@@ -193,19 +193,34 @@ int hmpc_ntt_inverse_plain(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uin
 
 /* --- batched transforms of uneven degree -------------------------------------
  * A batch of polynomials of different degrees (powers of two >= 8), each in
- * its own limb-planar buffer, transformed by ONE persistent kernel launch
- * replayed from a captured CUDA graph.  The reference runs one transform per
- * polynomial type (the degree is a template parameter, poly_mod.hpp:12-75).
- * With autotune != 0 the register radix (4 or 8 elements per thread), the
- * stages per shared-memory pass and the coalescing width are chosen by timing
- * the candidates on the device at creation.  Same results as
- * hmpc_ntt_forward / hmpc_ntt_inverse per polynomial. */
+ * its own limb-planar buffer, transformed from ONE captured CUDA graph.  The
+ * reference runs one transform per polynomial type (the degree is a template
+ * parameter, poly_mod.hpp:12-75).  Two engines:
+ *  - CUDA cores: one persistent kernel launch over every polynomial; its
+ *    register radix (4 or 8 elements per thread), stages per shared-memory
+ *    pass and coalescing width are a tile shape;
+ *  - tensor cores (moduli the tensor-core transform covers, every degree
+ *    >= 16, buffers 16-byte aligned): the polynomials bucketed by degree, each
+ *    bucket one tensor-core transform whose first group reads and last group
+ *    writes the polynomials' own buffers through device pointer tables.
+ * autotune: HMPC_BATCH_DEFAULT (the CUDA-core default tile shape),
+ * HMPC_BATCH_AUTOTUNE (time every CUDA-core tile shape and the tensor-core
+ * engine on the device at creation and keep the fastest) or
+ * HMPC_BATCH_TENSOR_CORES (the tensor-core engine; HMPC_ERROR_UNSUPPORTED
+ * when it does not cover the batch).  Same results as hmpc_ntt_forward /
+ * hmpc_ntt_inverse per polynomial. */
+#define HMPC_BATCH_DEFAULT 0
+#define HMPC_BATCH_AUTOTUNE 1
+#define HMPC_BATCH_TENSOR_CORES 2
 typedef struct hmpc_ntt_batch hmpc_ntt_batch;
 int hmpc_ntt_batch_create(hmpc_context* ctx, hmpc_modulus* mod, uint64_t count, const uint64_t* degrees, int inverse,
                           int autotune, hmpc_ntt_batch** out);
 /* in[i] / out[i]: degrees[i]*L words each (in[i] may equal out[i]); ordered
  * on the context's stream. */
 int hmpc_ntt_batch_run(hmpc_ntt_batch* batch, const uint32_t* const* in, uint32_t* const* out);
+/* The engine and tile shape the batch runs with (radix_bits 0: the
+ * tensor-core engine, local_bits its split), the CUDA-core kernel's work
+ * items or the tensor-core graph's kernel launches, and the tuned time. */
 int hmpc_ntt_batch_info(const hmpc_ntt_batch* batch, int* radix_bits, int* local_bits, int* col_bits, uint32_t* items,
                         float* tuned_ms);
 /* After a run: waits for it and reports whether every work item finished

@@ -1,5 +1,5 @@
 """Parity of the tensor-core transform engine (tile shape radix bits 0) with
-the CPU oracle: bit-exact forward and inverse transforms, fused CBD(V)
+the CPU oracle for moduli of 2 to 8 limbs: bit-exact forward and inverse transforms, fused CBD(V)
 samplers, ragged batches, in-place calls, and the fallback to the CUDA-core
 tiles for calls the engine does not cover."""
 import numpy as np
@@ -15,7 +15,11 @@ Q_256 = 0xCFF479B9B12CCF05AF55BCA0D7AE005D53E20D920B577D2785F3A1F156740001  # L=
 Q_128 = 0xE78EC7A9E37BEFBFF59DF3057EBC0001  # L=4
 Q_NTT = 0x18F25CD9A75CCBD9C146D4ABAEC00001  # examples/ntt.cpp:22, L=4, 125 bits
 P_64 = 0x8822D80623320001  # tests/expr/crypto/lhe/enc.cpp:16, L=2
-Q_192 = 0x8605423C957246B58997DEC24F688AB3DD46CB31C5700001  # L=6: not covered by the engine
+Q_96 = 0x800000000000000002060001  # L=3
+Q_160 = 0x92155E09E949EDD961C374C93DE4B90B9F220001  # L=5
+Q_192 = 0x8605423C957246B58997DEC24F688AB3DD46CB31C5700001  # L=6
+Q_224 = 0xE9E9C9C7700173EE913AE1871AE48451A42CE7E731BC0F8A00C20001  # L=7
+Q_288 = (1 << 287) + 0x5E0001  # an odd 9-limb modulus: not covered by the engine
 
 
 @pytest.fixture(scope="module")
@@ -46,7 +50,7 @@ def tensor_plan(gm, n, batch, inverse=False):
     assert gm.plan(n, batch, inverse)["radix_bits"] == 0
 
 
-@pytest.mark.parametrize("q", [Q_256, Q_128, Q_NTT, P_64])
+@pytest.mark.parametrize("q", [Q_256, Q_128, Q_NTT, P_64, Q_96, Q_160, Q_192, Q_224])
 @pytest.mark.parametrize("n,batch", [(16, 3), (32, 1), (64, 5), (1 << 10, 2), (1 << 12, 130), (1 << 13, 3)])
 def test_forward_and_inverse_match_oracle(queue, oracle, q, n, batch, cpu_threads):
     om = oracle.Modulus(q)
@@ -65,7 +69,7 @@ def test_forward_and_inverse_match_oracle(queue, oracle, q, n, batch, cpu_thread
     assert _lib.call("hmpc_context_synchronize", queue.handle) == 0
 
 
-@pytest.mark.parametrize("q", [Q_256, Q_128, P_64])
+@pytest.mark.parametrize("q", [Q_256, Q_128, P_64, Q_96, Q_160, Q_192, Q_224])
 @pytest.mark.parametrize("vx2", [1, 7, 20, 64])
 def test_fused_cbd_matches_oracle(queue, oracle, q, vx2, cpu_threads):
     om = oracle.Modulus(q)
@@ -102,7 +106,7 @@ def test_full_size_bgv_transform(queue, oracle, cpu_threads):
     assert (z.data == big.data).all().item()
 
 
-@pytest.mark.parametrize("q", [Q_256, P_64])
+@pytest.mark.parametrize("q", [Q_256, P_64, Q_192, Q_224])
 @pytest.mark.parametrize("n,batch", [(64, 5), (1 << 12, 130)])
 def test_unsplit_contiguous_group(queue, oracle, q, n, batch, cpu_threads):
     """the forward transform's last group and the inverse's first with one
@@ -142,9 +146,9 @@ def test_uncovered_calls_fall_back(queue, oracle):
     queue.nonce = [1, 2, 3]
     y = queue.ntt_uniform(gm, n, (batch,))
     assert np.array_equal(y.numpy(), oracle.ntt(om, n, batch, sampler="uniform", key=KEY, nonce=[1, 2, 3]))
-    g192 = queue.modulus(Q_192)
+    g288 = queue.modulus(Q_288)
     with pytest.raises(_lib.HmpcError):
-        g192.set_plan(n, batch, False, radix_bits=0)
+        g288.set_plan(n, batch, False, radix_bits=0)
     small = Tensor.from_numpy(gm, random_residues(oracle, om, 8 * 2, 3), (2,), 8)
     gm.set_plan(8, 2, False, radix_bits=0)
     assert np.array_equal(queue.ntt(small).numpy(), oracle.ntt(om, 8, 2, src=small.numpy()))
