@@ -485,18 +485,33 @@ def secondary_metrics(queue, int_peak):
     # continuous batching against plain per-request launches on the same stream
     from hmpc_gb300.serving import Server, poisson_stream, prepare, replay
 
-    for rate in (2000.0, 10000.0):
-        arrivals = poisson_stream(4000, rate=rate, seed=1)
+    # The mix has 75 compatibility classes (kind x degree x modulus), so two
+    # requests that may share a launch rarely arrive close together: the mix
+    # runs with no batching window (dispatch at once; the gain over plain
+    # launches is the overlap of four lanes) and with a 500 us window to show
+    # what holding for compatible arrivals costs.  A single-class stream
+    # (encryptions of one shape under one key) shows the same loop batching.
+    from hmpc_gb300.serving import REQUEST_ENCRYPT
+
+    modes = (("continuous_batching", 4, 16, 0), ("continuous_batching_window_500us", 4, 16, 500),
+             ("plain_per_request", 1, 1, 0))
+    streams = [(f"serving_poisson_{int(rate)}", dict(rate=rate), modes) for rate in (2000.0, 10000.0)]
+    streams.append(("serving_single_class_encrypt_n8192_q256_20000", dict(
+        rate=20000.0, log_n=(13, 13), counts=(1, 1), moduli=["q256"], kinds=(REQUEST_ENCRYPT,)),
+        (("continuous_batching", 4, 16, 0), ("continuous_batching_window_200us", 4, 16, 200),
+         ("plain_per_request", 1, 1, 0))))
+    for name, kw, stream_modes in streams:
+        arrivals = poisson_stream(4000, seed=1, **kw)
         p_mod, keys, shapes = prepare(queue, arrivals, slots=4)
-        serving = {"requests": len(arrivals), "offered_rate": rate}
-        for mode, lanes, max_batch in (("continuous_batching", 4, 16), ("plain_per_request", 1, 1)):
-            server = Server(queue, memory_budget=4 << 30, lanes=lanes, max_batch=max_batch)
+        serving = {"requests": len(arrivals), "offered_rate": kw["rate"]}
+        for mode, lanes, max_batch, window in stream_modes:
+            server = Server(queue, memory_budget=4 << 30, lanes=lanes, max_batch=max_batch, batch_window_us=window)
             _, wall, st = replay(queue, server, arrivals, p_mod, keys, shapes)
             server.close()
             serving[mode] = {"throughput_req_s": st["completed"] / wall, "p50_ms": st["p50_us"] / 1e3,
                              "p99_ms": st["p99_us"] / 1e3, "mean_batch": st["mean_batch"],
                              "completed": st["completed"], "rejected": st["rejected"], "launches": st["launches"]}
-        out[f"serving_poisson_{int(rate)}"] = serving
+        out[name] = serving
         del shapes, keys
 
     # wire format: the 256 ciphertexts of a batch as 512 per-polynomial

@@ -59,7 +59,13 @@ struct hmpc_ntt_batch
         uint64_t n = 0;
         std::vector<uint32_t> polys;
         size_t table = 0;  // offset of its in-pointers in the tables (out-pointers follow)
+        size_t digits = 0; // offset of its digit buffers
     };
+    // the buckets run side by side in the graph (one stream each, forked
+    // from and joined to the batch stream), each with digit buffers of its own
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> joins;
+    cudaEvent_t fork = nullptr;
     bool tc = false;
     std::vector<Bucket> buckets;
     void** d_tables = nullptr;  // device pointer tables
@@ -102,6 +108,19 @@ struct hmpc_ntt_batch
             cudaStreamSynchronize(stream);
         }
         release_plan();
+        for (cudaStream_t st : side)
+        {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+        for (cudaEvent_t ev : joins)
+        {
+            cudaEventDestroy(ev);
+        }
+        if (fork)
+        {
+            cudaEventDestroy(fork);
+        }
         if (start)
         {
             cudaEventDestroy(start);
@@ -170,8 +189,22 @@ struct hmpc_ntt_batch
             {
                 return rc;
             }
-            digit_words = std::max<uint64_t>(digit_words, per_element * n * bk.polys.size());
+            bk.digits = digit_words;
+            digit_words += (per_element * n * bk.polys.size() + 63) & ~uint64_t{63};
             buckets.push_back(std::move(bk));
+        }
+        while (side.size() < buckets.size())
+        {
+            cudaStream_t st = nullptr;
+            cudaEvent_t ev = nullptr;
+            HMPC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "creating a bucket stream");
+            side.push_back(st);
+            HMPC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "creating a bucket event");
+            joins.push_back(ev);
+        }
+        if (!fork)
+        {
+            HMPC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "creating the fork event");
         }
         HMPC_CUDA(cudaMalloc(&d_tables, table_entries * sizeof(void*)), "allocating pointer tables");
         HMPC_CUDA(cudaMallocHost(&h_tables, table_entries * sizeof(void*)), "allocating pointer tables");
@@ -195,16 +228,32 @@ struct hmpc_ntt_batch
         cudaGraph_t graph = nullptr;
         HMPC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capturing batch graph");
         int rc = HMPC_OK;
-        for (const Bucket& bk : buckets)
+        cudaError_t ce = cudaEventRecord(fork, stream);
+        for (size_t b = 0; b < buckets.size() && !rc && ce == cudaSuccess; ++b)
         {
-            auto** table = d_tables + bk.table;
-            rc = run_tc_polys(ctx, mod, bk.n, bk.polys.size(), inverse, local_bits,
-                              reinterpret_cast<const uint32_t* const*>(table),
-                              reinterpret_cast<uint32_t* const*>(table + bk.polys.size()), d_digits, stream);
-            if (rc)
+            const Bucket& bk = buckets[b];
+            ce = cudaStreamWaitEvent(side[b], fork, 0);
+            if (ce != cudaSuccess)
             {
                 break;
             }
+            auto** table = d_tables + bk.table;
+            rc = run_tc_polys(ctx, mod, bk.n, bk.polys.size(), inverse, local_bits,
+                              reinterpret_cast<const uint32_t* const*>(table),
+                              reinterpret_cast<uint32_t* const*>(table + bk.polys.size()),
+                              d_digits ? d_digits + bk.digits : nullptr, side[b]);
+            if (!rc)
+            {
+                ce = cudaEventRecord(joins[b], side[b]);
+            }
+            if (!rc && ce == cudaSuccess)
+            {
+                ce = cudaStreamWaitEvent(stream, joins[b], 0);
+            }
+        }
+        if (!rc && ce != cudaSuccess)
+        {
+            rc = cuda_fail(ce, "capturing batch graph");
         }
         items = static_cast<uint32_t>(ctx->launches - launches_before);
         ctx->launches = launches_before;

@@ -139,6 +139,7 @@ struct hmpc_server
     std::vector<Dispatch> lane_work;
     std::vector<bool> lane_busy;
     uint32_t desc_capacity = 0;              // polynomials per lane descriptor buffer
+    uint32_t batch_window_us = 0;            // hold a group that is not full for compatible arrivals
     uint32_t* d_desc = nullptr;              // device descriptors, one region per lane
     uint8_t* pool_base = nullptr;
     Pool pool;
@@ -431,13 +432,21 @@ struct hmpc_server
                     break;
                 }
                 std::deque<Request*>* best = nullptr;
+                const auto now = std::chrono::steady_clock::now();
                 for (auto& kv : pending)
                 {
-                    if (!kv.second.empty() &&
-                        (!best || kv.second.front()->submitted < best->front()->submitted))
+                    if (kv.second.empty() || (best && kv.second.front()->submitted >= best->front()->submitted))
                     {
-                        best = &kv.second;
+                        continue;
                     }
+                    // a group that could still grow waits for the window to pass
+                    // since its oldest request arrived
+                    if (batch_window_us && kv.second.size() < max_batch &&
+                        now - kv.second.front()->submitted < std::chrono::microseconds(batch_window_us))
+                    {
+                        continue;
+                    }
+                    best = &kv.second;
                 }
                 if (!best)
                 {
@@ -523,6 +532,7 @@ int hmpc_server_create(hmpc_context* ctx, const hmpc_server_config* config, hmpc
     srv->ctx = ctx;
     srv->max_batch = config->max_batch;
     srv->desc_capacity = config->max_batch_polynomials ? config->max_batch_polynomials : 4096;
+    srv->batch_window_us = config->batch_window_us;
     for (uint32_t i = 0; i < config->lanes; ++i)
     {
         auto lane = std::make_unique<hmpc_context>();

@@ -17,7 +17,8 @@ QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, -2
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("memory_budget_bytes", ctypes.c_uint64), ("lanes", ctypes.c_uint32),
-                ("max_batch", ctypes.c_uint32), ("max_batch_polynomials", ctypes.c_uint32)]
+                ("max_batch", ctypes.c_uint32), ("max_batch_polynomials", ctypes.c_uint32),
+                ("batch_window_us", ctypes.c_uint32)]
 
 
 class Request(ctypes.Structure):
@@ -63,10 +64,11 @@ class Server:
     """A serving loop on the queue's device.  max_batch=1, lanes=1 gives plain
     per-request launches (every request alone, one after the other)."""
 
-    def __init__(self, queue, memory_budget=1 << 30, lanes=4, max_batch=16, max_batch_polynomials=0):
+    def __init__(self, queue, memory_budget=1 << 30, lanes=4, max_batch=16, max_batch_polynomials=0,
+                 batch_window_us=0):
         self.lib = _bind()
         self.queue = queue
-        cfg = ServerConfig(memory_budget, lanes, max_batch, max_batch_polynomials)
+        cfg = ServerConfig(memory_budget, lanes, max_batch, max_batch_polynomials, batch_window_us)
         handle = ctypes.c_void_p()
         _lib.check(self.lib.hmpc_server_create(queue.handle, ctypes.byref(cfg), ctypes.byref(handle)))
         self.handle = handle
@@ -142,18 +144,20 @@ class Arrival:
 SERVING_MODULI = ["q128", "q160", "q192", "q224", "q256"]  # 4..8 limbs
 
 
-def poisson_stream(count, rate=2000.0, seed=1, log_n=(12, 16), counts=(1, 4), moduli=SERVING_MODULI):
+def poisson_stream(count, rate=2000.0, seed=1, log_n=(12, 16), counts=(1, 4), moduli=SERVING_MODULI,
+                   kinds=(REQUEST_NTT, REQUEST_ENCRYPT, REQUEST_CT_MUL)):
     """Seeded request stream: exponential inter-arrival times (mean 1/rate),
-    kind uniform over {NTT, encrypt, ct x ct}, degree uniform over
-    {2^log_n[0]..2^log_n[1]}, modulus uniform over 4..8 limbs, polynomial
-    count uniform over counts (all from one ChaCha20 stream)."""
+    kind uniform over `kinds` (NTT, encrypt, ct x ct), degree uniform over
+    {2^log_n[0]..2^log_n[1]}, modulus uniform over `moduli` (4..8 limbs),
+    polynomial count uniform over counts (all from one ChaCha20 stream)."""
     words = chacha20_words([0x5E5E0000 + seed] + [0] * 7, 5 * count)
     out, t = [], 0.0
     for i in range(count):
         w = words[5 * i:5 * i + 5]
         u = (w[0] + 0.5) / 2.0 ** 32
         t += -math.log(u) / rate
-        out.append(Arrival(t, w[1] % 3, log_n[0] + w[2] % (log_n[1] - log_n[0] + 1), moduli[w[3] % len(moduli)],
+        out.append(Arrival(t, kinds[w[1] % len(kinds)], log_n[0] + w[2] % (log_n[1] - log_n[0] + 1),
+                           moduli[w[3] % len(moduli)],
                            counts[0] + w[4] % (counts[1] - counts[0] + 1), i))
     return out
 

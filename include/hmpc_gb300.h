@@ -397,6 +397,8 @@ typedef struct hmpc_server_config
     uint32_t lanes;                  /* device streams, one dispatch each */
     uint32_t max_batch;              /* requests per dispatch (1: no batching) */
     uint32_t max_batch_polynomials;  /* polynomials per dispatch (0: 4096) */
+    uint32_t batch_window_us;        /* hold a group smaller than max_batch until its oldest request has */
+                                     /* waited this long, so compatible arrivals join it (0: at once) */
 } hmpc_server_config;
 
 #define HMPC_REQUEST_NTT 0       /* out0 = NTT(in0): count polynomials of degree n mod q */

@@ -122,3 +122,30 @@ def test_admission_by_memory(queue):
         ct = lhe.enc(queue, key, m, q)
         assert (ct.c0.data == o[0].data).all().item() and (ct.c1.data == o[1].data).all().item()
     server.close()
+
+
+def test_batching_window_groups_compatible_requests(queue):
+    """With a window, compatible requests submitted close together share
+    dispatches (mean batch above one) and each result still equals the
+    request's encryption alone."""
+    p = queue.modulus(MODULI["p64"])
+    q = queue.modulus(MODULI["q256"])
+    n = 1 << 11
+    q.prepare(n)
+    p.prepare(n)
+    _, key = lhe.keygen(queue, q, p, n)
+    server = Server(queue, memory_budget=1 << 28, lanes=2, max_batch=8, batch_window_us=20000)
+    kid = server.add_key(q, p, key)
+    msgs = [queue.uniform(p, (1,), n) for _ in range(16)]
+    outs = [(Tensor(q, (1,), n), Tensor(q, (1,), n)) for _ in range(16)]
+    queue.wait()
+    tickets = [server.submit_encrypt(kid, q, m, o[0], o[1], [100 + i, 0, 0]) for i, (m, o) in enumerate(zip(msgs, outs))]
+    server.drain()
+    st = server.stats()
+    server.close()
+    assert st["completed"] == 16 and st["mean_batch"] > 1.0
+    for i, (m, o) in enumerate(zip(msgs, outs)):
+        queue.nonce = [100 + i, 0, 0]
+        ct = lhe.enc(queue, key, m, q)
+        assert (ct.c0.data == o[0].data).all().item() and (ct.c1.data == o[1].data).all().item()
+    assert all(t is not None for t in tickets)
