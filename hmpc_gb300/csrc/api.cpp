@@ -160,6 +160,29 @@ namespace hmpc_gb300::detail
             }
             choice = hmpc_modulus::TileChoice{};
         }
+        if (choice.radix_bits == 1)
+        {
+            // one thread-block cluster per polynomial; calls it does not cover
+            // run the default CUDA-core tiles
+            if (kind == producer_tensor && !poly_rng && log_n >= 10 && log_n <= 14)
+            {
+                ClusterNttParams cp{};
+                cp.in = src;
+                cp.out = out;
+                cp.twiddles = inverse ? t->inverse : t->forward;
+                cp.elements = n * batch;
+                cp.log_n = static_cast<uint32_t>(log_n);
+                cp.inverse = inverse ? 1u : 0u;
+                cudaError_t e = mod->kt->ntt_cluster(cp, batch, mod->h, ctx->stream);
+                if (e != cudaSuccess)
+                {
+                    return cuda_fail(e, "launching the cluster transform");
+                }
+                ++ctx->launches;
+                return HMPC_OK;
+            }
+            choice = hmpc_modulus::TileChoice{};
+        }
         PlanOptions options;
         options.max_local_bits = choice.local_bits;
         options.col_bits = choice.col_bits;
@@ -718,6 +741,12 @@ int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inv
                                                 "0.996 * 2^(32L) whose top limb is at least 32");
         }
     }
+    else if (radix_bits == 1)
+    {
+        // the cluster engine has no tile shape
+        local_bits = 0;
+        col_bits = 0;
+    }
     else if ((radix_bits != 2 && radix_bits != 3) || local_bits < 0 || local_bits > 13 || col_bits < 0 ||
              col_bits > 6 ||
              (local_bits && static_cast<uint64_t>(mod->c.limbs) * 4u * smem_words(1u << local_bits) > 200 * 1024))
@@ -807,6 +836,20 @@ int hmpc_modulus_tune(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse
                 best = sample;
                 best_choice = tensor;
             }
+        }
+    }
+    if (log_n >= 10 && log_n <= 14 && batch <= 64)
+    {
+        // one thread-block cluster per polynomial
+        hmpc_modulus::TileChoice cluster;
+        cluster.radix_bits = 1;
+        cluster.local_bits = 0;
+        cluster.col_bits = 0;
+        const float sample = time_choice(cluster);
+        if (sample < best)
+        {
+            best = sample;
+            best_choice = cluster;
         }
     }
     for (int R : {3, 2})

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "chacha.cuh"
+#include "cluster.cuh"
 #include "linalg.cuh"
 #include "ntt.cuh"
 #include "plain.cuh"
@@ -91,6 +92,9 @@ namespace hmpc_gb300
                               uint32_t top_mask, unsigned grid, const HostModulus& m, cudaStream_t stream);
         cudaError_t (*equal)(uint32_t* out, const uint32_t* a, const uint32_t* b, uint64_t elements,
                              cudaStream_t stream);
+        // one thread-block cluster per polynomial (cluster.cuh), degrees 2^10..2^14
+        cudaError_t (*ntt_cluster)(const ClusterNttParams& p, uint64_t batch, const HostModulus& m,
+                                   cudaStream_t stream);
     };
 
     // sizes of one tensor-core group kernel instantiation (TcShape)

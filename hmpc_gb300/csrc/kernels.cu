@@ -415,10 +415,34 @@ namespace hmpc_gb300
             return cudaGetLastError();
         }
 
+        cudaError_t ntt_cluster(const ClusterNttParams& p, uint64_t batch, const HostModulus& h, cudaStream_t stream)
+        {
+            if (batch == 0)
+            {
+                return cudaSuccess;
+            }
+            if (p.log_n < 10 || p.log_n > 14)
+            {
+                return cudaErrorInvalidValue;
+            }
+            const size_t smem = cl_smem_bytes<L>(p.log_n);
+            static cudaError_t configured = cudaFuncSetAttribute(
+                ntt_cluster_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cl_smem_bytes<L>(14)));
+            if (configured != cudaSuccess)
+            {
+                return configured;
+            }
+            // one radix-8 group of the widest round per thread
+            const uint32_t work = 1u << (p.log_n - 6);
+            const unsigned threads = std::min(256u, std::max(32u, work));
+            ntt_cluster_kernel<L><<<static_cast<unsigned>(batch * cl_ctas), threads, smem, stream>>>(p, device_modulus(h));
+            return cudaGetLastError();
+        }
+
         const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd, to_montgomery,
                                    from_montgomery, cast, plain_stage, ct_mul, dec_combine, ntt_batched,
                                    ntt_batched_blocks_per_sm, R, lhe_combine_pair, matvec, matvec_monomial,
-                                   reduce, equal};
+                                   reduce, equal, ntt_cluster};
     }
 
     const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()

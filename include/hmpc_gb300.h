@@ -104,7 +104,10 @@ int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root
  * fp16 MMAs over 8-bit digits, moduli of 2 to 8 limbs below
  * 0.996 * 2^(32L); tensor and CBD(V) producers; other calls of that shape
  * run the default tiles), whose local_bits selects the output split (1 or 2,
- * 0 = 1) of the group with contiguous rows.  No counterpart in the reference (its transform
+ * 0 = 1) of the group with contiguous rows; or radix bits 1: one thread-block
+ * cluster of 8 CTAs per polynomial holding it in distributed shared memory,
+ * one launch per transform (degrees 2^10..2^14, tensor producer; other calls
+ * run the default tiles).  No counterpart in the reference (its transform
  * has one schedule).  hmpc_modulus_tune times the candidates on the device
  * (scratch buffers, values irrelevant to the cost) and keeps the fastest. */
 int hmpc_modulus_set_plan(hmpc_modulus* mod, uint64_t n, uint64_t batch, int inverse, int radix_bits, int local_bits,
