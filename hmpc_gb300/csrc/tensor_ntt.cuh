@@ -247,11 +247,14 @@ namespace hmpc_gb300
             const TcRow r = tc_row<S::g>(p, h, mt, row);
             const uint32_t* rp = p.in + r.base;
             uint64_t stride = p.elements;
-            if (p.in_polys)
+            if constexpr (IN == tc_in_limbs)
             {
-                // the row's polynomial in its own buffer (read only for rows in range)
-                stride = 1ull << p.log_n;
-                rp = r.ok ? p.in_polys[r.poly] + (r.base & (stride - 1ull)) : p.in;
+                if (p.in_polys)
+                {
+                    // the row's polynomial in its own buffer (read only for rows in range)
+                    stride = 1ull << p.log_n;
+                    rp = r.ok ? p.in_polys[r.poly] + (r.base & (stride - 1ull)) : p.in;
+                }
             }
             const bool contiguous = p.lo == 0;  // the row's R elements are adjacent: vector loads
 #pragma unroll
@@ -724,10 +727,13 @@ namespace hmpc_gb300
         const uint32_t k0 = split * outputs + kl0;   // its element index in the group
         uint32_t* op = p.out + r.base;
         uint64_t ostride = p.elements;
-        if (p.out_polys)
+        if constexpr (OUT == tc_out_limbs)
         {
-            ostride = 1ull << p.log_n;
-            op = r.ok ? p.out_polys[r.poly] + (r.base & (ostride - 1ull)) : p.out;
+            if (p.out_polys)
+            {
+                ostride = 1ull << p.log_n;
+                op = r.ok ? p.out_polys[r.poly] + (r.base & (ostride - 1ull)) : p.out;
+            }
         }
         uint32_t res[Contig ? words_out : 1][Contig ? per : 1];
 #pragma unroll
