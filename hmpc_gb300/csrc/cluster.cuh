@@ -42,21 +42,63 @@ namespace hmpc_gb300
     };
 
     // shared memory of one CTA: two buffers of N/8 elements (element-major),
-    // one per layout, so the exchange never writes a buffer still being read
+    // one per layout, so the exchange never writes a buffer still being read,
+    // and the CTA's twiddles (N/8 + 7 entries, loaded once at the start)
     template<int L>
     __host__ __device__ constexpr size_t cl_smem_bytes(uint32_t log_n)
     {
-        return 2ull * (1ull << (log_n - 3)) * L * sizeof(uint32_t);
+        return (3ull * (1ull << (log_n - 3)) + 8ull) * L * sizeof(uint32_t);
+    }
+
+    // Shared-memory slot of the twiddle of stage s for the butterfly whose
+    // first element is e.  Slots 0..7 hold T[0..7] (the three stages on the
+    // top index bits use only these); the stages inside CTA `rank`'s block
+    // use 2^(stage's depth) consecutive entries each, stored after them.
+    struct ClTwiddles
+    {
+        uint32_t log_n, inverse;
+
+        // global table index
+        __device__ __forceinline__ uint32_t index(uint32_t s, uint32_t e) const
+        {
+            return inverse ? (1u << (log_n - s - 1)) + (e >> (s + 1)) : (1u << s) + (e >> (log_n - s));
+        }
+
+        // slot: top-bit stages map to their index (0..7); block stages to
+        // 8 + (2^d - 1) + (index - first index of the stage in this CTA's
+        // block), d the number of bits of the index below the block bits
+        __device__ __forceinline__ uint32_t slot(uint32_t s, uint32_t e) const
+        {
+            const uint32_t kb = log_n - 3;
+            const bool block = inverse ? s < kb : s >= 3;
+            if (!block)
+            {
+                return index(s, e);
+            }
+            const uint32_t d = inverse ? kb - s - 1 : s - 3;  // index bits from the local part of e
+            return 8u + (1u << d) - 1u + (index(s, e) & ((1u << d) - 1u));
+        }
+    };
+
+    template<int L>
+    __device__ __forceinline__ void cl_twiddle(uint32_t (&t)[L], const uint32_t* tw, uint32_t slot)
+    {
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+        {
+            t[j] = tw[slot * L + j];
+        }
     }
 
     template<int L>
     __device__ __forceinline__ void cl_butterfly(uint32_t (&u)[L], uint32_t (&v)[L], const ClusterNttParams& p,
-                                                 const Modulus<L>& m, uint32_t s, uint32_t e)
+                                                 const Modulus<L>& m, uint32_t s, uint32_t e, const uint32_t* tw)
     {
+        const ClTwiddles tws{p.log_n, p.inverse};
         uint32_t t[L], x[L];
         if (!p.inverse)
         {
-            load_twiddle<L>(t, p.twiddles, (1u << s) + (e >> (p.log_n - s)));
+            cl_twiddle<L>(t, tw, tws.slot(s, e));
             mont_mul<L>(v, v, t, m);
             mod_add<L>(x, u, v, m);
             mod_sub<L>(v, u, v, m);
@@ -68,7 +110,7 @@ namespace hmpc_gb300
         }
         else if (s + 1 < p.log_n)
         {
-            load_twiddle<L>(t, p.twiddles, (1u << (p.log_n - s - 1)) + (e >> (s + 1)));
+            cl_twiddle<L>(t, tw, tws.slot(s, e));
             uint32_t d[L];
             mod_add<L>(x, u, v, m);
             mod_sub<L>(d, u, v, m);
@@ -84,9 +126,9 @@ namespace hmpc_gb300
             uint32_t d[L];
             mod_add<L>(x, u, v, m);
             mod_sub<L>(d, u, v, m);
-            load_twiddle<L>(t, p.twiddles, 0);
+            cl_twiddle<L>(t, tw, 0);
             mont_mul<L>(u, x, t, m);
-            load_twiddle<L>(t, p.twiddles, 1);
+            cl_twiddle<L>(t, tw, 1);
             mont_mul<L>(v, d, t, m);
         }
     }
@@ -95,7 +137,8 @@ namespace hmpc_gb300
     // (index bit `bit0` upwards in the inverse, downwards in the forward)
     template<int L, int G>
     __device__ __forceinline__ void cl_stages(uint32_t (&x)[1 << G][L], const ClusterNttParams& p,
-                                              const Modulus<L>& m, uint32_t s0, uint32_t e0, uint32_t bit0)
+                                              const Modulus<L>& m, uint32_t s0, uint32_t e0, uint32_t bit0,
+                                              const uint32_t* tw)
     {
 #pragma unroll
         for (int st = 0; st < G; ++st)
@@ -110,7 +153,7 @@ namespace hmpc_gb300
                     continue;
                 }
                 const uint32_t e = e0 + (static_cast<uint32_t>(i) << bit0);
-                cl_butterfly<L>(x[i], x[i | (1 << b)], p, m, s0 + static_cast<uint32_t>(st), e);
+                cl_butterfly<L>(x[i], x[i | (1 << b)], p, m, s0 + static_cast<uint32_t>(st), e, tw);
             }
         }
     }
@@ -141,7 +184,8 @@ namespace hmpc_gb300
     // the CTA's block buffer or global memory.
     template<int L, int G, bool FromGlobal, bool ToGlobal>
     __device__ __forceinline__ void cl_block_round(const ClusterNttParams& p, const Modulus<L>& m, uint32_t* blk,
-                                                   uint32_t rank, uint64_t base, uint32_t s0, uint32_t bit0)
+                                                   uint32_t rank, uint64_t base, uint32_t s0, uint32_t bit0,
+                                                   const uint32_t* tw)
     {
         const uint32_t kb = p.log_n - 3;
         const uint32_t groups = 1u << (kb - G);
@@ -169,7 +213,7 @@ namespace hmpc_gb300
                     cl_read<L>(x[i], blk, l);
                 }
             }
-            cl_stages<L, G>(x, p, m, s0, e0, bit0);
+            cl_stages<L, G>(x, p, m, s0, e0, bit0, tw);
 #pragma unroll
             for (int i = 0; i < (1 << G); ++i)
             {
@@ -202,8 +246,31 @@ namespace hmpc_gb300
         const uint32_t slice = B >> 3;        // low values per CTA in the top-bit layout
         uint32_t* blk = cl_smem;              // block layout: local index l of element (rank << kb) | l
         uint32_t* top = cl_smem + B * L;      // top-bit layout: element (h << kb) | (rank * slice + g) at g * 8 + h
+        uint32_t* tw = cl_smem + 2 * B * L;   // twiddle slots (ClTwiddles::slot)
         const uint32_t rank = cluster.block_rank();
         const uint64_t base = static_cast<uint64_t>(blockIdx.x / cl_ctas) << k;
+        // the CTA's twiddles: T[0..7], then per block stage its 2^d entries
+        // starting at the index of the block's first butterfly
+        {
+            const ClTwiddles tws{k, p.inverse};
+            const uint32_t slots = B + 7u;
+            for (uint32_t i = threadIdx.x; i < slots * L; i += blockDim.x)
+            {
+                const uint32_t sl = i / L, j = i % L;
+                uint32_t index = sl;
+                if (sl >= 8)
+                {
+                    // slot 8 + 2^d - 1 + o: depth d, offset o
+                    const uint32_t r = sl - 7u;                  // 2^d + o, o < 2^d
+                    const uint32_t d = 31u - __clz(r);
+                    const uint32_t o = r - (1u << d);
+                    const uint32_t s = p.inverse ? kb - 1u - d : d + 3u;
+                    index = tws.index(s, rank << kb) + o;
+                }
+                tw[i] = p.twiddles[static_cast<uint64_t>(index) * L + j];
+            }
+            __syncthreads();
+        }
         // every CTA of the cluster runs before any writes into its shared memory
         cluster.sync();
         if (!p.inverse)
@@ -223,7 +290,7 @@ namespace hmpc_gb300
                         x[h][j] = p.in[static_cast<uint64_t>(j) * p.elements + base + (static_cast<uint64_t>(h) << kb) + l];
                     }
                 }
-                cl_stages<L, 3>(x, p, m, 0, l, kb);
+                cl_stages<L, 3>(x, p, m, 0, l, kb, tw);
 #pragma unroll
                 for (int h = 0; h < 8; ++h)
                 {
@@ -235,21 +302,21 @@ namespace hmpc_gb300
             uint32_t s = 3;
             while (k - s > 3)
             {
-                cl_block_round<L, 3, false, false>(p, m, blk, rank, base, s, k - s - 3);
+                cl_block_round<L, 3, false, false>(p, m, blk, rank, base, s, k - s - 3, tw);
                 __syncthreads();
                 s += 3;
             }
             if (k - s == 3)
             {
-                cl_block_round<L, 3, false, true>(p, m, blk, rank, base, s, 0);
+                cl_block_round<L, 3, false, true>(p, m, blk, rank, base, s, 0, tw);
             }
             else if (k - s == 2)
             {
-                cl_block_round<L, 2, false, true>(p, m, blk, rank, base, s, 0);
+                cl_block_round<L, 2, false, true>(p, m, blk, rank, base, s, 0, tw);
             }
             else
             {
-                cl_block_round<L, 1, false, true>(p, m, blk, rank, base, s, 0);
+                cl_block_round<L, 1, false, true>(p, m, blk, rank, base, s, 0, tw);
             }
         }
         else
@@ -259,20 +326,20 @@ namespace hmpc_gb300
             const uint32_t first = kb % 3 ? kb % 3 : 3;
             if (first == 3)
             {
-                cl_block_round<L, 3, true, false>(p, m, blk, rank, base, 0, 0);
+                cl_block_round<L, 3, true, false>(p, m, blk, rank, base, 0, 0, tw);
             }
             else if (first == 2)
             {
-                cl_block_round<L, 2, true, false>(p, m, blk, rank, base, 0, 0);
+                cl_block_round<L, 2, true, false>(p, m, blk, rank, base, 0, 0, tw);
             }
             else
             {
-                cl_block_round<L, 1, true, false>(p, m, blk, rank, base, 0, 0);
+                cl_block_round<L, 1, true, false>(p, m, blk, rank, base, 0, 0, tw);
             }
             for (uint32_t s = first; s < kb; s += 3)
             {
                 __syncthreads();
-                cl_block_round<L, 3, false, false>(p, m, blk, rank, base, s, s);
+                cl_block_round<L, 3, false, false>(p, m, blk, rank, base, s, s, tw);
             }
             __syncthreads();
             // each element to the CTA that holds its slice of low values
@@ -294,7 +361,7 @@ namespace hmpc_gb300
                 {
                     cl_read<L>(x[h], top, g * 8 + h);
                 }
-                cl_stages<L, 3>(x, p, m, kb, l, kb);
+                cl_stages<L, 3>(x, p, m, kb, l, kb, tw);
 #pragma unroll
                 for (int h = 0; h < 8; ++h)
                 {

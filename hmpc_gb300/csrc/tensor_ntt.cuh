@@ -929,12 +929,15 @@ namespace hmpc_gb300
                 constexpr int ks_total = S::k_pad / 16;
                 constexpr int ks_half = NBUF == 1 ? (ks_total + 1) / 2 : ks_total;
                 constexpr uint32_t h0_bytes = NBUF == 1 ? 2u * ks_half * S::lbo_b : S::b_bytes;
-                // copies issued and waited for per barrier: on an abort the copies
-                // still in flight are waited for (bounded) before the CTA exits
-                uint32_t issued[2] = {0u, 0u}, landed[2] = {0u, 0u};
+                // copies issued and waited for per barrier (scalars: an indexed
+                // array would live in local memory on this thread's issue path):
+                // on an abort the copies still in flight are waited for
+                // (bounded) before the CTA exits
+                uint32_t issued0 = 0, issued1 = 0, landed0 = 0, landed1 = 0;
                 auto copy = [&](uint32_t jb, uint32_t piece) {
                     // NBUF 2: piece = buffer (whole image); NBUF 1: piece = K half
-                    ++issued[piece];
+                    issued0 += piece == 0u ? 1u : 0u;
+                    issued1 += piece != 0u ? 1u : 0u;
                     const uint8_t* src = p.images + (hb_first + jb) * S::b_bytes;
                     if constexpr (NBUF == 2)
                     {
@@ -1015,7 +1018,8 @@ namespace hmpc_gb300
                             give_up(1);
                             break;
                         }
-                        ++landed[piece0];
+                        landed0 += piece0 == 0u ? 1u : 0u;
+                        landed1 += piece0 != 0u ? 1u : 0u;
                     }
                     tc::fence_after_sync();
                     const uint32_t a0 = tc::smem_u32(sa);
@@ -1036,7 +1040,7 @@ namespace hmpc_gb300
                                 give_up(1);
                                 break;
                             }
-                            ++landed[1];
+                            ++landed1;
                         }
                         tc::fence_after_sync();
 #pragma unroll
@@ -1057,12 +1061,13 @@ namespace hmpc_gb300
                     // at most one copy per barrier is in flight (the next one into a
                     // buffer is issued after the previous one was waited for): let
                     // it land before the shared memory is released
-                    for (uint32_t piece = 0; piece < 2; ++piece)
+                    if (issued0 > landed0)
                     {
-                        if (issued[piece] > landed[piece])
-                        {
-                            tc::mbar_wait(&bar_b[piece], landed[piece] & 1u, p.spin_limit);
-                        }
+                        tc::mbar_wait(&bar_b[0], landed0 & 1u, p.spin_limit);
+                    }
+                    if (issued1 > landed1)
+                    {
+                        tc::mbar_wait(&bar_b[1], landed1 & 1u, p.spin_limit);
                     }
                 }
             }
