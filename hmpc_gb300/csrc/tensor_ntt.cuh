@@ -1079,13 +1079,27 @@ namespace hmpc_gb300
             static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
             // word-major K where rows are columns of strided elements; the
             // contiguous last group measured faster with digit-major K
+            // Groups whose rows are adjacent elements (8 worker warps, a long
+            // carry-out per tile) keep the loads of two tiles in flight: a
+            // second register set takes tile i + 2 while tile i + 1 is stored.
+            // The strided groups (16 warps) keep one.
+            constexpr bool deep = Contig && !S::generated;
             TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig> loader;
+            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig> loader2;
             TcCursor cur = first;
             if constexpr (!S::generated)
             {
                 if (count)
                 {
                     loader.load(p, cur.hb / NS, cur.mt, tid);
+                }
+                if constexpr (deep)
+                {
+                    if (count > 1)
+                    {
+                        const TcCursor n1 = cur.next(tpb);
+                        loader2.load(p, n1.hb / NS, n1.mt, tid);
+                    }
                 }
             }
             TcCursor prev = cur;
@@ -1116,13 +1130,40 @@ namespace hmpc_gb300
                     {
                         tc_store_small(p, sa, cur.mt, tid);
                     }
+                    else if constexpr (deep)
+                    {
+                        // register sets alternate by tile (static indexing keeps them in registers)
+                        if ((i & 1u) == 0)
+                        {
+                            loader.store(sa, tid);
+                        }
+                        else
+                        {
+                            loader2.store(sa, tid);
+                        }
+                    }
                     else
                     {
                         loader.store(sa, tid);
                     }
                     tc::fence_proxy_async();
                     mbar_arrive(bar_a_full);
-                    if constexpr (!S::generated)
+                    if constexpr (deep)
+                    {
+                        if (i + 2 < count)
+                        {
+                            const TcCursor n2 = cur.next(tpb).next(tpb);
+                            if ((i & 1u) == 0)
+                            {
+                                loader.load(p, n2.hb / NS, n2.mt, tid);
+                            }
+                            else
+                            {
+                                loader2.load(p, n2.hb / NS, n2.mt, tid);
+                            }
+                        }
+                    }
+                    else if constexpr (!S::generated)
                     {
                         if (i + 1 < count)
                         {
