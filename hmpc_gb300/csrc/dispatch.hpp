@@ -110,6 +110,7 @@ namespace hmpc_gb300
     {
         int digits;
         // layout bit 0: the input digit planes are blocked per row, bit 1: the output
+        // planes; bit 2: limb input / output through per-polynomial pointer tables
         cudaError_t (*group)(const TcGroupParams& p, int r, int in_kind, int out_kind, int splits, int layout,
                              unsigned grid, cudaStream_t stream);
         bool (*shape)(int r, int in_kind, int out_kind, int splits, TcShapeInfo& out);

@@ -413,15 +413,18 @@ namespace hmpc_gb300::detail
             const unsigned grid =
                 static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
             const int splits = first_sampled ? 1 : static_cast<int>(gp.shape.splits);
-            if (j == 0)
+            int layout = gp.layout;
+            if (j == 0 && in_polys)
             {
                 p.in_polys = in_polys;
+                layout |= 4;
             }
-            if (j + 1 == tt->groups.size())
+            if (j + 1 == tt->groups.size() && out_polys)
             {
                 p.out_polys = out_polys;
+                layout |= 4;
             }
-            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, gp.layout, grid, stream);
+            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, layout, grid, stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching a tensor-core transform group");

@@ -73,46 +73,58 @@ namespace hmpc_gb300
         }
 
         // the instantiated shapes: every (R, input, output, splits, contiguous,
-        // record layout) a plan uses
-        template<typename F>
-        bool dispatch(int r, int in_kind, int out_kind, int splits, bool contig, int lay, F& f)
+        // record layout) a plan uses; P: the limb input / output in one buffer
+        // per polynomial (layout bit 2), for the shapes that read or write limbs
+        template<bool P, typename F>
+        bool dispatch_shapes(int r, int in_kind, int out_kind, int splits, bool contig, int lay, F& f)
         {
+            constexpr int X = P ? 4 : 0;
             if (out_kind == tc_out_digits && r == 8 && !contig && splits == 1)
             {
-                if (in_kind == tc_in_limbs) return lay ? f.template run<8, tc_in_limbs, tc_out_digits, 1, false, 2>()
-                                                       : f.template run<8, tc_in_limbs, tc_out_digits, 1, false, 0>();
-                if (in_kind == tc_in_cbd) return lay ? f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 2>()
-                                                     : f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 0>();
-                if (in_kind == tc_in_small) return lay ? f.template run<8, tc_in_small, tc_out_digits, 1, false, 2>()
-                                                       : f.template run<8, tc_in_small, tc_out_digits, 1, false, 0>();
-                if (in_kind == tc_in_digits) return lay ? f.template run<8, tc_in_digits, tc_out_digits, 1, false, 2>()
-                                                        : f.template run<8, tc_in_digits, tc_out_digits, 1, false, 0>();
+                if (in_kind == tc_in_limbs) return lay ? f.template run<8, tc_in_limbs, tc_out_digits, 1, false, 2 | X>()
+                                                       : f.template run<8, tc_in_limbs, tc_out_digits, 1, false, X>();
+                if constexpr (!P)
+                {
+                    if (in_kind == tc_in_cbd) return lay ? f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 2>()
+                                                         : f.template run<8, tc_in_cbd, tc_out_digits, 1, false, 0>();
+                    if (in_kind == tc_in_small) return lay ? f.template run<8, tc_in_small, tc_out_digits, 1, false, 2>()
+                                                           : f.template run<8, tc_in_small, tc_out_digits, 1, false, 0>();
+                    if (in_kind == tc_in_digits) return lay ? f.template run<8, tc_in_digits, tc_out_digits, 1, false, 2>()
+                                                            : f.template run<8, tc_in_digits, tc_out_digits, 1, false, 0>();
+                }
             }
             if (out_kind == tc_out_digits && r == 8 && contig && in_kind == tc_in_limbs && lay == 0)
             {
-                if (splits == 2) return f.template run<8, tc_in_limbs, tc_out_digits, 2, true, 0>();
-                if (splits == 1) return f.template run<8, tc_in_limbs, tc_out_digits, 1, true, 0>();
+                if (splits == 2) return f.template run<8, tc_in_limbs, tc_out_digits, 2, true, X>();
+                if (splits == 1) return f.template run<8, tc_in_limbs, tc_out_digits, 1, true, X>();
             }
             if (out_kind == tc_out_limbs && in_kind == tc_in_digits)
             {
                 if (lay == 1 && contig && splits == 1)
                 {
-                    if (r == 8) return f.template run<8, tc_in_digits, tc_out_limbs, 1, true, 1>();
-                    if (r == 4) return f.template run<4, tc_in_digits, tc_out_limbs, 1, true, 1>();
-                    if (r == 2) return f.template run<2, tc_in_digits, tc_out_limbs, 1, true, 1>();
+                    if (r == 8) return f.template run<8, tc_in_digits, tc_out_limbs, 1, true, 1 | X>();
+                    if (r == 4) return f.template run<4, tc_in_digits, tc_out_limbs, 1, true, 1 | X>();
+                    if (r == 2) return f.template run<2, tc_in_digits, tc_out_limbs, 1, true, 1 | X>();
                 }
                 if (lay == 0)
                 {
-                    if (r == 8 && splits == 2 && contig) return f.template run<8, tc_in_digits, tc_out_limbs, 2, true, 0>();
-                    if (r == 8 && splits == 1) return contig ? f.template run<8, tc_in_digits, tc_out_limbs, 1, true, 0>()
-                                                             : f.template run<8, tc_in_digits, tc_out_limbs, 1, false, 0>();
-                    if (r == 4 && splits == 1) return contig ? f.template run<4, tc_in_digits, tc_out_limbs, 1, true, 0>()
-                                                             : f.template run<4, tc_in_digits, tc_out_limbs, 1, false, 0>();
-                    if (r == 2 && splits == 1) return contig ? f.template run<2, tc_in_digits, tc_out_limbs, 1, true, 0>()
-                                                             : f.template run<2, tc_in_digits, tc_out_limbs, 1, false, 0>();
+                    if (r == 8 && splits == 2 && contig) return f.template run<8, tc_in_digits, tc_out_limbs, 2, true, X>();
+                    if (r == 8 && splits == 1) return contig ? f.template run<8, tc_in_digits, tc_out_limbs, 1, true, X>()
+                                                             : f.template run<8, tc_in_digits, tc_out_limbs, 1, false, X>();
+                    if (r == 4 && splits == 1) return contig ? f.template run<4, tc_in_digits, tc_out_limbs, 1, true, X>()
+                                                             : f.template run<4, tc_in_digits, tc_out_limbs, 1, false, X>();
+                    if (r == 2 && splits == 1) return contig ? f.template run<2, tc_in_digits, tc_out_limbs, 1, true, X>()
+                                                             : f.template run<2, tc_in_digits, tc_out_limbs, 1, false, X>();
                 }
             }
             return false;
+        }
+
+        template<typename F>
+        bool dispatch(int r, int in_kind, int out_kind, int splits, bool contig, int lay, F& f)
+        {
+            return (lay & 4) ? dispatch_shapes<true>(r, in_kind, out_kind, splits, contig, lay & 3, f)
+                             : dispatch_shapes<false>(r, in_kind, out_kind, splits, contig, lay & 3, f);
         }
 
         struct Launcher

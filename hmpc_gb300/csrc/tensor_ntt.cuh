@@ -233,7 +233,8 @@ namespace hmpc_gb300
     // InBlk: the input digit planes are blocked per R adjacent elements (word w
     // of element e at (e - e mod R) * W + w * R + e mod R): a row is one run
     // WordMajor: r = 8 tiles take the word-major K order of tc_k_index
-    template<int DC, int R, int IN, int NS, int Parts, bool InBlk = false, bool WordMajor = false>
+    // Polys: the group's limb input is one buffer per polynomial (in_polys)
+    template<int DC, int R, int IN, int NS, int Parts, bool InBlk = false, bool WordMajor = false, bool Polys = false>
     struct TcLoader
     {
         using S = TcShape<DC, R, IN, NS>;
@@ -247,14 +248,11 @@ namespace hmpc_gb300
             const TcRow r = tc_row<S::g>(p, h, mt, row);
             const uint32_t* rp = p.in + r.base;
             uint64_t stride = p.elements;
-            if constexpr (IN == tc_in_limbs)
+            if constexpr (Polys && IN == tc_in_limbs)
             {
-                if (p.in_polys)
-                {
-                    // the row's polynomial in its own buffer (read only for rows in range)
-                    stride = 1ull << p.log_n;
-                    rp = r.ok ? p.in_polys[r.poly] + (r.base & (stride - 1ull)) : p.in;
-                }
+                // the row's polynomial in its own buffer (read only for rows in range)
+                stride = 1ull << p.log_n;
+                rp = r.ok ? p.in_polys[r.poly] + (r.base & (stride - 1ull)) : p.in;
             }
             const bool contiguous = p.lo == 0;  // the row's R elements are adjacent: vector loads
 #pragma unroll
@@ -703,7 +701,7 @@ namespace hmpc_gb300
     // and `per` consecutive output elements of the block's split; Contig: the
     // row's elements are adjacent (no column bits), stored as vectors;
     // ByteCarry: the two-operation carry (inputs other than limbs)
-    template<int DC, int R, int OUT, int NS, bool Contig, bool OutRec, bool ByteCarry>
+    template<int DC, int R, int OUT, int NS, bool Contig, bool OutRec, bool ByteCarry, bool Polys>
     __device__ __forceinline__ void tc_epilogue(const TcGroupParams& p, uint32_t tmem, const TcCursor& cur,
                                                 uint32_t warp, uint32_t lane)
     {
@@ -727,13 +725,11 @@ namespace hmpc_gb300
         const uint32_t k0 = split * outputs + kl0;   // its element index in the group
         uint32_t* op = p.out + r.base;
         uint64_t ostride = p.elements;
-        if constexpr (OUT == tc_out_limbs)
+        if constexpr (Polys && OUT == tc_out_limbs)
         {
-            if (p.out_polys)
-            {
-                ostride = 1ull << p.log_n;
-                op = r.ok ? p.out_polys[r.poly] + (r.base & (ostride - 1ull)) : p.out;
-            }
+            // the row's polynomial in its own buffer (written only for rows in range)
+            ostride = 1ull << p.log_n;
+            op = r.ok ? p.out_polys[r.poly] + (r.base & (ostride - 1ull)) : p.out;
         }
         uint32_t res[Contig ? words_out : 1][Contig ? per : 1];
 #pragma unroll
@@ -840,7 +836,8 @@ namespace hmpc_gb300
     // buffers (transaction count).  Every wait is bounded; a timeout sets the
     // error word and both sides leave their loops.
     // Lay bit 0: the input digit planes are blocked per R adjacent elements;
-    // bit 1: the output planes are blocked for the next group
+    // bit 1: the output planes are blocked for the next group; bit 2: limb
+    // input or output in one buffer per polynomial (in_polys / out_polys)
     template<int DC, int R, int IN, int OUT, int NS, bool Contig, int Lay>
     __global__ void __launch_bounds__(tc_workers<Contig> + 32, 1) tc_group_kernel(const TcGroupParams p)
     {
@@ -1079,27 +1076,13 @@ namespace hmpc_gb300
             static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
             // word-major K where rows are columns of strided elements; the
             // contiguous last group measured faster with digit-major K
-            // Groups whose rows are adjacent elements (8 worker warps, a long
-            // carry-out per tile) keep the loads of two tiles in flight: a
-            // second register set takes tile i + 2 while tile i + 1 is stored.
-            // The strided groups (16 warps) keep one.
-            constexpr bool deep = Contig && !S::generated;
-            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig> loader;
-            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig> loader2;
+            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig, (Lay & 4) != 0> loader;
             TcCursor cur = first;
             if constexpr (!S::generated)
             {
                 if (count)
                 {
                     loader.load(p, cur.hb / NS, cur.mt, tid);
-                }
-                if constexpr (deep)
-                {
-                    if (count > 1)
-                    {
-                        const TcCursor n1 = cur.next(tpb);
-                        loader2.load(p, n1.hb / NS, n1.mt, tid);
-                    }
                 }
             }
             TcCursor prev = cur;
@@ -1130,40 +1113,13 @@ namespace hmpc_gb300
                     {
                         tc_store_small(p, sa, cur.mt, tid);
                     }
-                    else if constexpr (deep)
-                    {
-                        // register sets alternate by tile (static indexing keeps them in registers)
-                        if ((i & 1u) == 0)
-                        {
-                            loader.store(sa, tid);
-                        }
-                        else
-                        {
-                            loader2.store(sa, tid);
-                        }
-                    }
                     else
                     {
                         loader.store(sa, tid);
                     }
                     tc::fence_proxy_async();
                     mbar_arrive(bar_a_full);
-                    if constexpr (deep)
-                    {
-                        if (i + 2 < count)
-                        {
-                            const TcCursor n2 = cur.next(tpb).next(tpb);
-                            if ((i & 1u) == 0)
-                            {
-                                loader.load(p, n2.hb / NS, n2.mt, tid);
-                            }
-                            else
-                            {
-                                loader2.load(p, n2.hb / NS, n2.mt, tid);
-                            }
-                        }
-                    }
-                    else if constexpr (!S::generated)
+                    if constexpr (!S::generated)
                     {
                         if (i + 1 < count)
                         {
@@ -1188,8 +1144,8 @@ namespace hmpc_gb300
                         break;
                     }
                     tc::fence_after_sync();
-                    tc_epilogue<DC, R, OUT, NS, Contig, (Lay & 2) != 0, IN != tc_in_limbs>(p, tmem + acc * S::cols,
-                                                                                          prev, warp, lane);
+                    tc_epilogue<DC, R, OUT, NS, Contig, (Lay & 2) != 0, IN != tc_in_limbs, (Lay & 4) != 0>(
+                        p, tmem + acc * S::cols, prev, warp, lane);
                     tc::fence_before_sync();
                     mbar_arrive(&bar_acc_empty[acc]);
                 }
