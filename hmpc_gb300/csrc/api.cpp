@@ -1170,11 +1170,9 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
         // in its first group, and p*NTT(w) one of p*w.  The three transforms
         // (u, p*v + lift(m), p*w) share every constant after their first
         // group, so they run stacked: three first-group launches, then the
-        // other groups once over 3 * batch polynomials.  The last group
-        // combines c0 = a*U + X and c1 = b*U + W' in its carry-out (or one
-        // combine kernel does where that group's rows are not adjacent
-        // elements); every result is the reduced representative, so the
-        // ciphertext is the reference's bit for bit.  RNG order as the
+        // other groups once over 3 * batch polynomials.  One combine reads u
+        // once and writes c0 and c1; every result is the reduced
+        // representative, so the ciphertext is the reference's bit for bit.  RNG order as the
         // reference's plan: u, v, w (expr/cache.hpp:226-271).
         int rc = HMPC_OK;
         const uint32_t* coefficients = plaintext;
@@ -1192,19 +1190,11 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
         parts[2].vx2 = 20;
         parts[2].small = &no_msg;
         uint32_t* stacked = ws;  // [L][3 * elements]: u | p*v + lift(m) | p*w, in NTT form
-        TcCombine comb;
-        comb.c0 = c0;
-        comb.c1 = c1;
-        comb.key_a = key_a;
-        comb.key_b = key_b;
-        comb.batch = batch;
-        bool combined = false;
         if (!rc)
         {
-            // the last group writes c0 and c1 itself where its rows are adjacent elements
-            rc = run_tc_stacked(ctx, q, n, batch, parts, 3, stacked, tc_splits, &comb, &combined);
+            rc = run_tc_stacked(ctx, q, n, batch, parts, 3, stacked, tc_splits);
         }
-        if (!rc && !combined)
+        if (!rc)
         {
             cudaError_t e = q->kt->lhe_combine_pair(c0, c1, key_a, key_b, n, stacked, elements, q->h, ctx->stream);
             if (e != cudaSuccess)

@@ -291,22 +291,8 @@ namespace hmpc_gb300::detail
         uint32_t vx2 = 0;
         const TcSmallInput* small = nullptr;  // nullptr: plain CBD(V) input
     };
-    // The BGV combine folded into the last group of three stacked parts
-    // (u, p*v + lift(m), p*w): c0 = a*U + X, c1 = b*U + W' written straight to
-    // the ciphertext (key polynomials a, b of degree n, Montgomery form).
-    struct TcCombine
-    {
-        uint32_t* c0 = nullptr;
-        uint32_t* c1 = nullptr;
-        const uint32_t* key_a = nullptr;
-        const uint32_t* key_b = nullptr;
-        uint64_t batch = 0;
-    };
-    // *combined: whether the last group wrote the ciphertext (else `out`
-    // holds the three transforms and the caller combines)
     int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
-                       int count, uint32_t* out, int splits, const TcCombine* comb = nullptr,
-                       bool* combined = nullptr);
+                       int count, uint32_t* out, int splits);
     int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out);
     // Polynomials of one degree n in buffers of their own (the batched
     // transform's buckets).  tc_prepare_polys builds the constants of (n,

@@ -369,10 +369,8 @@ namespace hmpc_gb300::detail
         }
 
         // group j over `batch` polynomials; stride = plane stride of the digit / limb planes
-        // comb: the last group of the stacked BGV transforms writes the combined
-        // ciphertext (batch = 3 * comb->batch stacked rows)
         int group(size_t j, const uint32_t* in, uint32_t* out, uint64_t stride, uint64_t batch, int in_kind,
-                  uint32_t vx2, const TcSmallInput* small, uint64_t msg_stride, const TcCombine* comb = nullptr)
+                  uint32_t vx2, const TcSmallInput* small, uint64_t msg_stride)
         {
             const TcGroupPlan& gp = tt->groups[j];
             const bool first_sampled = j == 0 && (in_kind == tc_in_cbd || in_kind == tc_in_small);
@@ -412,25 +410,8 @@ namespace hmpc_gb300::detail
                     p.phalf[i] = pm->c.half[static_cast<size_t>(i)];
                 }
             }
-            int out_kind = gp.out_kind;
-            uint64_t units = p.tiles;
-            if (comb)
-            {
-                // tiles in triples (X, W', U of 128 polynomials), one triple at least per CTA
-                out_kind = tc_out_combine;
-                p.out = comb->c0;
-                p.out2 = comb->c1;
-                p.key_a = comb->key_a;
-                p.key_b = comb->key_b;
-                p.qninv = mod->c.ninv;
-                p.comb_batch = static_cast<uint32_t>(comb->batch);
-                p.elements = comb->batch << log_n;
-                p.tiles_per_block = static_cast<uint32_t>(3 * ((comb->batch + tc_rows - 1) / tc_rows));
-                p.tiles = gp.blocks * p.tiles_per_block;
-                units = p.tiles / 3;
-            }
             const unsigned grid =
-                static_cast<unsigned>(std::min<uint64_t>(units, static_cast<uint64_t>(ctx->sm_count)));
+                static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
             const int splits = first_sampled ? 1 : static_cast<int>(gp.shape.splits);
             int layout = gp.layout;
             if (j == 0 && in_polys)
@@ -443,7 +424,7 @@ namespace hmpc_gb300::detail
                 p.out_polys = out_polys;
                 layout |= 4;
             }
-            cudaError_t e = k->group(p, 1 << gp.g, in_kind, out_kind, splits, layout, grid, stream);
+            cudaError_t e = k->group(p, 1 << gp.g, in_kind, gp.out_kind, splits, layout, grid, stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching a tensor-core transform group");
@@ -510,12 +491,8 @@ namespace hmpc_gb300::detail
     }
 
     int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
-                       int count, uint32_t* out, int splits, const TcCombine* comb, bool* combined)
+                       int count, uint32_t* out, int splits)
     {
-        if (combined)
-        {
-            *combined = false;
-        }
         bool need_cbd = false, need_small = false;
         for (int i = 0; i < count; ++i)
         {
@@ -566,24 +543,15 @@ namespace hmpc_gb300::detail
             }
             nonce_add(ctx->nonce, elements);
         }
-        // the shared groups over the stacked batch; the last one combines the
-        // ciphertext when its rows are adjacent elements read from blocked planes
-        const TcGroupPlan& last = tt->groups.back();
-        const bool fuse = comb && count == 3 && stages >= 2 && last.lo == 0 && (last.layout & 1) &&
-                          last.shape.splits == 1;
+        // the shared groups over the stacked batch
         for (size_t j = 1; j < stages; ++j)
         {
             const uint32_t* in = digits + (((j - 1) & 1u) ? w * total : 0);
             uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * total : 0);
-            const TcCombine* c = fuse && j + 1 == stages ? comb : nullptr;
-            if (int rc = run.group(j, in, o, total, batch * static_cast<uint64_t>(count), tc_in_digits, 0, nullptr, 0, c))
+            if (int rc = run.group(j, in, o, total, batch * static_cast<uint64_t>(count), tc_in_digits, 0, nullptr, 0))
             {
                 return rc;
             }
-        }
-        if (combined)
-        {
-            *combined = fuse;
         }
         return HMPC_OK;
     }

@@ -2,8 +2,7 @@
 // -DHMPC_L=<2..8>; exports tc_kernels_<L>().  Instantiated group shapes:
 // the first group (r = 8) from limbs or from centred binomial samples, the
 // middle groups (r = 8) digits to digits, the last group (r = 2, 4 or 8)
-// digits to reduced limbs (or, for the stacked BGV transforms, to the
-// combined ciphertext).
+// digits to reduced limbs.
 #include <mutex>
 
 #include "dispatch.hpp"
@@ -98,15 +97,6 @@ namespace hmpc_gb300
             {
                 if (splits == 2) return f.template run<8, tc_in_limbs, tc_out_digits, 2, true, X>();
                 if (splits == 1) return f.template run<8, tc_in_limbs, tc_out_digits, 1, true, X>();
-            }
-            if constexpr (!P)
-            {
-                if (out_kind == tc_out_combine && in_kind == tc_in_digits && lay == 1 && contig && splits == 1)
-                {
-                    if (r == 8) return f.template run<8, tc_in_digits, tc_out_combine, 1, true, 1>();
-                    if (r == 4) return f.template run<4, tc_in_digits, tc_out_combine, 1, true, 1>();
-                    if (r == 2) return f.template run<2, tc_in_digits, tc_out_combine, 1, true, 1>();
-                }
             }
             if (out_kind == tc_out_limbs && in_kind == tc_in_digits)
             {

@@ -64,9 +64,6 @@ namespace hmpc_gb300
     {
         tc_out_digits = 0,
         tc_out_limbs = 1,
-        // the last group of the stacked BGV transforms (rows: U, X, W' of each
-        // polynomial): reduced limbs combined into c0 = a*U + X, c1 = b*U + W'
-        tc_out_combine = 2,
     };
 
     constexpr int tc_rows = 128;
@@ -111,14 +108,6 @@ namespace hmpc_gb300
         // batch is one buffer of `elements` words per plane)
         const uint32_t* const* in_polys;
         uint32_t* const* out_polys;
-        // tc_out_combine: out = c0, out2 = c1 (plane stride `elements` =
-        // batch * N), the key polynomials (N words per plane, Montgomery form),
-        // -q^-1 mod 2^32 and the batch (the stacked input holds 3 * batch rows)
-        uint32_t* out2;
-        const uint32_t* key_a;
-        const uint32_t* key_b;
-        uint32_t qninv;
-        uint32_t comb_batch;
     };
 
     // base-256 digits of the small-integer input (|x| < 2^70 for p < 2^64, 2V <= 64):
@@ -226,39 +215,16 @@ namespace hmpc_gb300
         bool ok;
         uint64_t base;  // element index of m = 0
         uint64_t poly;
-        // Comb: the output element of m = 0 and the row's part (0: X, 1: W', 2: U)
-        uint64_t out_base;
-        uint32_t part;
     };
 
-    // Comb (the combining last group, rows adjacent elements): the tiles of a
-    // block come in triples over 128 polynomials -- X, then W', then U -- so
-    // that the thread that carries out U of an element wrote X and W' of the
-    // same element two and one tiles before (the stacked input holds U, X,
-    // W' of every polynomial at rows 0, batch, 2 batch)
-    template<int G, bool Comb = false>
+    template<int G>
     __device__ __forceinline__ TcRow tc_row(const TcGroupParams& p, uint64_t h, uint32_t mt, uint32_t row)
     {
+        const uint64_t rho = static_cast<uint64_t>(mt) * tc_rows + row;
         TcRow r;
-        if constexpr (Comb)
-        {
-            const uint32_t t = mt / 3u;
-            r.part = mt - 3u * t;
-            const uint64_t poly = static_cast<uint64_t>(t) * tc_rows + row;
-            r.ok = poly < p.comb_batch;
-            r.poly = (r.part == 2u ? 0ull : (r.part + 1ull) * p.comb_batch) + poly;
-            r.base = (r.poly << p.log_n) + (h << G);
-            r.out_base = (poly << p.log_n) + (h << G);
-        }
-        else
-        {
-            const uint64_t rho = static_cast<uint64_t>(mt) * tc_rows + row;
-            r.ok = rho < p.rows;
-            r.poly = rho >> p.lo;
-            r.base = (r.poly << p.log_n) + (h << (p.lo + G)) + (rho & ((1ull << p.lo) - 1ull));
-            r.out_base = r.base;
-            r.part = 0;
-        }
+        r.ok = rho < p.rows;
+        r.poly = rho >> p.lo;
+        r.base = (r.poly << p.log_n) + (h << (p.lo + G)) + (rho & ((1ull << p.lo) - 1ull));
         return r;
     }
 
@@ -268,8 +234,7 @@ namespace hmpc_gb300
     // of element e at (e - e mod R) * W + w * R + e mod R): a row is one run
     // WordMajor: r = 8 tiles take the word-major K order of tc_k_index
     // Polys: the group's limb input is one buffer per polynomial (in_polys)
-    template<int DC, int R, int IN, int NS, int Parts, bool InBlk = false, bool WordMajor = false, bool Polys = false,
-             bool Comb = false>
+    template<int DC, int R, int IN, int NS, int Parts, bool InBlk = false, bool WordMajor = false, bool Polys = false>
     struct TcLoader
     {
         using S = TcShape<DC, R, IN, NS>;
@@ -280,7 +245,7 @@ namespace hmpc_gb300
         __device__ __forceinline__ void load(const TcGroupParams& p, uint64_t h, uint32_t mt, uint32_t tid)
         {
             const uint32_t row = tid % tc_rows, part = tid / tc_rows;
-            const TcRow r = tc_row<S::g, Comb>(p, h, mt, row);
+            const TcRow r = tc_row<S::g>(p, h, mt, row);
             const uint32_t* rp = p.in + r.base;
             uint64_t stride = p.elements;
             if constexpr (Polys && IN == tc_in_limbs)
@@ -732,93 +697,6 @@ namespace hmpc_gb300
         }
     }
 
-    template<int Per>
-    __device__ __forceinline__ void load_run(const uint32_t* p, uint32_t (&v)[Per])
-    {
-        if constexpr (Per == 4)
-        {
-            const uint4 a = *reinterpret_cast<const uint4*>(p);
-            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        }
-        else if constexpr (Per == 2)
-        {
-            const uint2 a = *reinterpret_cast<const uint2*>(p);
-            v[0] = a.x; v[1] = a.y;
-        }
-        else
-        {
-            v[0] = p[0];
-        }
-    }
-
-    // The BGV combine of hmpc's enc (expr/crypto/lhe/enc.hpp:65-68, with p*v +
-    // lift(m) and p*w transformed as inputs of their own): a row of X is
-    // stored as c0 and a row of W' as c1; a row of U (two tiles later, same
-    // thread and elements) reads them back and writes c0 = a*U + X and
-    // c1 = b*U + W' -- Montgomery products with the key coefficient of each
-    // element, then modular additions: the fully reduced results.
-    template<int L, int Per>
-    __device__ __forceinline__ void tc_combine(const TcGroupParams& p, const TcRow& r, uint32_t k0,
-                                               const uint32_t (&y)[L][Per])
-    {
-        const uint64_t e0 = r.out_base + k0;
-        if (r.part < 2u)
-        {
-            uint32_t* dst = (r.part == 0u ? p.out : p.out2) + e0;
-#pragma unroll
-            for (int w = 0; w < L; ++w)
-            {
-                store_run<Per>(dst + w * p.elements, y[w]);
-            }
-            return;
-        }
-        Modulus<L> m;
-#pragma unroll
-        for (int j = 0; j < L; ++j)
-        {
-            m.q[j] = p.q[j];
-        }
-        m.ninv = p.qninv;
-        const uint64_t mask = (1ull << p.log_n) - 1ull;
-#pragma unroll
-        for (int half = 0; half < 2; ++half)
-        {
-            uint32_t* dst = (half == 0 ? p.out : p.out2) + e0;
-            const uint32_t* key = half == 0 ? p.key_a : p.key_b;
-            uint32_t acc[L][Per];
-#pragma unroll
-            for (int w = 0; w < L; ++w)
-            {
-                load_run<Per>(dst + w * p.elements, acc[w]);
-            }
-#pragma unroll
-            for (int kk = 0; kk < Per; ++kk)
-            {
-                const uint64_t kc = (e0 + kk) & mask;
-                uint32_t a[L], u[L], x[L];
-#pragma unroll
-                for (int w = 0; w < L; ++w)
-                {
-                    a[w] = __ldg(key + (static_cast<uint64_t>(w) << p.log_n) + kc);
-                    u[w] = y[w][kk];
-                    x[w] = acc[w][kk];
-                }
-                mont_mul<L>(a, a, u, m);
-                mod_add<L>(x, x, a, m);
-#pragma unroll
-                for (int w = 0; w < L; ++w)
-                {
-                    acc[w][kk] = x[w];
-                }
-            }
-#pragma unroll
-            for (int w = 0; w < L; ++w)
-            {
-                store_run<Per>(dst + w * p.elements, acc[w]);
-            }
-        }
-    }
-
     // carry the accumulator of one tile out of TMEM: each thread owns one row
     // and `per` consecutive output elements of the block's split; Contig: the
     // row's elements are adjacent (no column bits), stored as vectors;
@@ -842,7 +720,7 @@ namespace hmpc_gb300
         const uint32_t row = 32u * lg + lane;
         const uint64_t h = cur.hb / NS;
         const uint32_t split = static_cast<uint32_t>(cur.hb % NS);
-        const TcRow r = tc_row<g, OUT == tc_out_combine>(p, h, cur.mt, row);
+        const TcRow r = tc_row<g>(p, h, cur.mt, row);
         const uint32_t kl0 = (warp >> 2) * per;      // first local output of this thread
         const uint32_t k0 = split * outputs + kl0;   // its element index in the group
         uint32_t* op = p.out + r.base;
@@ -931,14 +809,7 @@ namespace hmpc_gb300
                 }
             }
         }
-        if constexpr (Contig && OUT == tc_out_combine)
-        {
-            if (r.ok)
-            {
-                tc_combine<L, per>(p, r, k0, res);
-            }
-        }
-        else if constexpr (Contig)
+        if constexpr (Contig)
         {
             if (r.ok)
             {
@@ -993,10 +864,8 @@ namespace hmpc_gb300
         const uint32_t tid = threadIdx.x;
         const uint32_t warp = tid >> 5, lane = tid & 31u;
 
-        // the combining group: whole triples of tiles per CTA (tc_row)
-        constexpr uint64_t unit = OUT == tc_out_combine ? 3u : 1u;
-        const uint64_t t_begin = unit * ((p.tiles / unit) * blockIdx.x / gridDim.x);
-        const uint64_t t_end = unit * ((p.tiles / unit) * (blockIdx.x + 1) / gridDim.x);
+        const uint64_t t_begin = p.tiles * blockIdx.x / gridDim.x;
+        const uint64_t t_end = p.tiles * (blockIdx.x + 1) / gridDim.x;
         const uint64_t count = t_end - t_begin;
         const uint32_t tpb = p.tiles_per_block;
         const uint64_t hb_first = t_begin / tpb;
@@ -1207,8 +1076,7 @@ namespace hmpc_gb300
             static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
             // word-major K where rows are columns of strided elements; the
             // contiguous last group measured faster with digit-major K
-            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig, (Lay & 4) != 0, OUT == tc_out_combine>
-                loader;
+            TcLoader<DC, R, IN, NS, tc_threads / tc_rows, in_blk, !Contig, (Lay & 4) != 0> loader;
             TcCursor cur = first;
             if constexpr (!S::generated)
             {
