@@ -14,10 +14,11 @@
 //    h * N/8 .. (h + 1) * N/8 - 1.
 // One all-to-all exchange through distributed shared memory moves every
 // element between the two layouts (forward: after the top stages; inverse:
-// before them).  Each thread applies up to three consecutive stages to eight
-// elements in registers (radix 8), with a CTA barrier between rounds inside
-// the block layout.  The values are the fully reduced representatives of the
-// reference's transform, bit for bit.
+// before them).  Every stage is one radix-2 butterfly per thread on shared
+// memory with a CTA barrier after it, so all of a CTA's threads take part
+// in every stage; the twiddles a CTA needs are preloaded into shared memory.
+// The values are the fully reduced representatives of the reference's
+// transform, bit for bit.
 #pragma once
 
 #include <cstdint>
@@ -133,31 +134,6 @@ namespace hmpc_gb300
         }
     }
 
-    // stages s0 .. s0 + G - 1 on the 2^G elements x[i] at indices e0 + i * dist
-    // (index bit `bit0` upwards in the inverse, downwards in the forward)
-    template<int L, int G>
-    __device__ __forceinline__ void cl_stages(uint32_t (&x)[1 << G][L], const ClusterNttParams& p,
-                                              const Modulus<L>& m, uint32_t s0, uint32_t e0, uint32_t bit0,
-                                              const uint32_t* tw)
-    {
-#pragma unroll
-        for (int st = 0; st < G; ++st)
-        {
-            // forward: the first stage pairs on the highest of the G bits
-            const int b = p.inverse ? st : G - 1 - st;
-#pragma unroll
-            for (int i = 0; i < (1 << G); ++i)
-            {
-                if (i & (1 << b))
-                {
-                    continue;
-                }
-                const uint32_t e = e0 + (static_cast<uint32_t>(i) << bit0);
-                cl_butterfly<L>(x[i], x[i | (1 << b)], p, m, s0 + static_cast<uint32_t>(st), e, tw);
-            }
-        }
-    }
-
     template<int L>
     __device__ __forceinline__ void cl_read(uint32_t (&x)[L], const uint32_t* sm, uint32_t local)
     {
@@ -178,60 +154,55 @@ namespace hmpc_gb300
         }
     }
 
-    // One round of G stages inside the block layout (CTA `rank` holds indices
-    // rank * B .. rank * B + B - 1): every thread group of 2^G elements whose
-    // local indices differ in bits bit0 .. bit0 + G - 1.  Source and sink are
-    // the CTA's block buffer or global memory.
-    template<int L, int G, bool FromGlobal, bool ToGlobal>
-    __device__ __forceinline__ void cl_block_round(const ClusterNttParams& p, const Modulus<L>& m, uint32_t* blk,
-                                                   uint32_t rank, uint64_t base, uint32_t s0, uint32_t bit0,
-                                                   const uint32_t* tw)
+    // index i with a zero bit inserted at position b
+    __device__ __forceinline__ uint32_t cl_spread(uint32_t i, uint32_t b)
+    {
+        return ((i >> b) << (b + 1)) | (i & ((1u << b) - 1u));
+    }
+
+    // One stage on the block layout (CTA `rank` holds elements (rank << kb) | l
+    // at local index l): butterflies on local index bit `bit`, one per thread
+    // and pass, then a CTA barrier.
+    template<int L>
+    __device__ __forceinline__ void cl_block_stage(const ClusterNttParams& p, const Modulus<L>& m, uint32_t* blk,
+                                                   uint32_t rank, uint32_t s, uint32_t bit, const uint32_t* tw)
     {
         const uint32_t kb = p.log_n - 3;
-        const uint32_t groups = 1u << (kb - G);
-        for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x)
+        for (uint32_t t = threadIdx.x; t < (1u << (kb - 1)); t += blockDim.x)
         {
-            // local index of element 0 of the group: g with G zero bits inserted at bit0
-            const uint32_t low = g & ((1u << bit0) - 1u);
-            const uint32_t l0 = ((g >> bit0) << (bit0 + G)) | low;
-            const uint32_t e0 = (rank << kb) | l0;
-            uint32_t x[1 << G][L];
-#pragma unroll
-            for (int i = 0; i < (1 << G); ++i)
-            {
-                const uint32_t l = l0 + (static_cast<uint32_t>(i) << bit0);
-                if constexpr (FromGlobal)
-                {
-#pragma unroll
-                    for (int j = 0; j < L; ++j)
-                    {
-                        x[i][j] = p.in[static_cast<uint64_t>(j) * p.elements + base + (rank << kb) + l];
-                    }
-                }
-                else
-                {
-                    cl_read<L>(x[i], blk, l);
-                }
-            }
-            cl_stages<L, G>(x, p, m, s0, e0, bit0, tw);
-#pragma unroll
-            for (int i = 0; i < (1 << G); ++i)
-            {
-                const uint32_t l = l0 + (static_cast<uint32_t>(i) << bit0);
-                if constexpr (ToGlobal)
-                {
-#pragma unroll
-                    for (int j = 0; j < L; ++j)
-                    {
-                        p.out[static_cast<uint64_t>(j) * p.elements + base + (rank << kb) + l] = x[i][j];
-                    }
-                }
-                else
-                {
-                    cl_write<L>(blk, l, x[i]);
-                }
-            }
+            const uint32_t lu = cl_spread(t, bit);
+            const uint32_t lv = lu | (1u << bit);
+            uint32_t u[L], v[L];
+            cl_read<L>(u, blk, lu);
+            cl_read<L>(v, blk, lv);
+            cl_butterfly<L>(u, v, p, m, s, (rank << kb) | lu, tw);
+            cl_write<L>(blk, lu, u);
+            cl_write<L>(blk, lv, v);
         }
+        __syncthreads();
+    }
+
+    // One stage on the top-bit layout (element (h << kb) | (rank * slice + g)
+    // at local index g * 8 + h): butterflies on bit `hb` of h.
+    template<int L>
+    __device__ __forceinline__ void cl_top_stage(const ClusterNttParams& p, const Modulus<L>& m, uint32_t* top,
+                                                 uint32_t rank, uint32_t s, uint32_t hb, const uint32_t* tw)
+    {
+        const uint32_t kb = p.log_n - 3;
+        const uint32_t slice = 1u << (kb - 3);
+        for (uint32_t t = threadIdx.x; t < slice * 4u; t += blockDim.x)
+        {
+            const uint32_t g = t >> 2;
+            const uint32_t hu = cl_spread(t & 3u, hb);
+            const uint32_t hv = hu | (1u << hb);
+            uint32_t u[L], v[L];
+            cl_read<L>(u, top, g * 8u + hu);
+            cl_read<L>(v, top, g * 8u + hv);
+            cl_butterfly<L>(u, v, p, m, s, (hu << kb) | (rank * slice + g), tw);
+            cl_write<L>(top, g * 8u + hu, u);
+            cl_write<L>(top, g * 8u + hv, v);
+        }
+        __syncthreads();
     }
 
     template<int L>
@@ -269,108 +240,88 @@ namespace hmpc_gb300
                 }
                 tw[i] = p.twiddles[static_cast<uint64_t>(index) * L + j];
             }
-            __syncthreads();
         }
-        // every CTA of the cluster runs before any writes into its shared memory
-        cluster.sync();
         if (!p.inverse)
         {
-            // stages 0..2 on the top bits, straight from global memory, then each
-            // element to the CTA that holds its block
-            for (uint32_t g = threadIdx.x; g < slice; g += blockDim.x)
+            // the CTA's slice of every top-bit group, coalesced along g
+            for (uint32_t i = threadIdx.x; i < B; i += blockDim.x)
             {
-                const uint32_t l = rank * slice + g;
-                uint32_t x[8][L];
+                const uint32_t g = i % slice, h = i / slice;
+                const uint64_t e = base + (static_cast<uint64_t>(h) << kb) + rank * slice + g;
 #pragma unroll
-                for (int h = 0; h < 8; ++h)
+                for (int j = 0; j < L; ++j)
                 {
-#pragma unroll
-                    for (int j = 0; j < L; ++j)
-                    {
-                        x[h][j] = p.in[static_cast<uint64_t>(j) * p.elements + base + (static_cast<uint64_t>(h) << kb) + l];
-                    }
+                    top[(g * 8u + h) * L + j] = p.in[static_cast<uint64_t>(j) * p.elements + e];
                 }
-                cl_stages<L, 3>(x, p, m, 0, l, kb, tw);
-#pragma unroll
-                for (int h = 0; h < 8; ++h)
-                {
-                    cl_write<L>(cluster.map_shared_rank(blk, h), l, x[h]);
-                }
+            }
+            __syncthreads();
+            // stages 0..2 on the top bits (bits 2, 1, 0 of h)
+            for (uint32_t s = 0; s < 3; ++s)
+            {
+                cl_top_stage<L>(p, m, top, rank, s, 2u - s, tw);
+            }
+            // every CTA runs before remote stores reach its shared memory
+            cluster.sync();
+            for (uint32_t i = threadIdx.x; i < B; i += blockDim.x)
+            {
+                const uint32_t g = i % slice, h = i / slice;
+                uint32_t x[L];
+                cl_read<L>(x, top, g * 8u + h);
+                cl_write<L>(cluster.map_shared_rank(blk, h), rank * slice + g, x);
             }
             cluster.sync();
-            // stages 3 .. k - 1 in the block layout, three per round
-            uint32_t s = 3;
-            while (k - s > 3)
+            // stages 3 .. k - 1 in the block layout (local bits kb - 1 .. 0)
+            for (uint32_t s = 3; s < k; ++s)
             {
-                cl_block_round<L, 3, false, false>(p, m, blk, rank, base, s, k - s - 3, tw);
-                __syncthreads();
-                s += 3;
+                cl_block_stage<L>(p, m, blk, rank, s, k - 1u - s, tw);
             }
-            if (k - s == 3)
+            for (uint32_t i = threadIdx.x; i < B; i += blockDim.x)
             {
-                cl_block_round<L, 3, false, true>(p, m, blk, rank, base, s, 0, tw);
-            }
-            else if (k - s == 2)
-            {
-                cl_block_round<L, 2, false, true>(p, m, blk, rank, base, s, 0, tw);
-            }
-            else
-            {
-                cl_block_round<L, 1, false, true>(p, m, blk, rank, base, s, 0, tw);
+#pragma unroll
+                for (int j = 0; j < L; ++j)
+                {
+                    p.out[static_cast<uint64_t>(j) * p.elements + base + (rank << kb) + i] = blk[i * L + j];
+                }
             }
         }
         else
         {
-            // stages 0 .. kb - 1 in the block layout (low bits first), the first
-            // round from global memory
-            const uint32_t first = kb % 3 ? kb % 3 : 3;
-            if (first == 3)
+            for (uint32_t i = threadIdx.x; i < B; i += blockDim.x)
             {
-                cl_block_round<L, 3, true, false>(p, m, blk, rank, base, 0, 0, tw);
-            }
-            else if (first == 2)
-            {
-                cl_block_round<L, 2, true, false>(p, m, blk, rank, base, 0, 0, tw);
-            }
-            else
-            {
-                cl_block_round<L, 1, true, false>(p, m, blk, rank, base, 0, 0, tw);
-            }
-            for (uint32_t s = first; s < kb; s += 3)
-            {
-                __syncthreads();
-                cl_block_round<L, 3, false, false>(p, m, blk, rank, base, s, s, tw);
+#pragma unroll
+                for (int j = 0; j < L; ++j)
+                {
+                    blk[i * L + j] = p.in[static_cast<uint64_t>(j) * p.elements + base + (rank << kb) + i];
+                }
             }
             __syncthreads();
+            // stages 0 .. kb - 1 in the block layout (local bits 0 .. kb - 1)
+            for (uint32_t s = 0; s < kb; ++s)
+            {
+                cl_block_stage<L>(p, m, blk, rank, s, s, tw);
+            }
+            cluster.sync();
             // each element to the CTA that holds its slice of low values
             for (uint32_t l = threadIdx.x; l < B; l += blockDim.x)
             {
                 uint32_t x[L];
                 cl_read<L>(x, blk, l);
-                const uint32_t c = l / slice;
-                cl_write<L>(cluster.map_shared_rank(top, c), (l % slice) * 8 + rank, x);
+                cl_write<L>(cluster.map_shared_rank(top, l / slice), (l % slice) * 8u + rank, x);
             }
             cluster.sync();
-            // stages kb .. k - 1 on the top bits, the last with the scaling
-            for (uint32_t g = threadIdx.x; g < slice; g += blockDim.x)
+            // stages kb .. k - 1 on the top bits (bits 0, 1, 2 of h), the last with the scaling
+            for (uint32_t s = kb; s < k; ++s)
             {
-                const uint32_t l = rank * slice + g;
-                uint32_t x[8][L];
+                cl_top_stage<L>(p, m, top, rank, s, s - kb, tw);
+            }
+            for (uint32_t i = threadIdx.x; i < B; i += blockDim.x)
+            {
+                const uint32_t g = i % slice, h = i / slice;
+                const uint64_t e = base + (static_cast<uint64_t>(h) << kb) + rank * slice + g;
 #pragma unroll
-                for (int h = 0; h < 8; ++h)
+                for (int j = 0; j < L; ++j)
                 {
-                    cl_read<L>(x[h], top, g * 8 + h);
-                }
-                cl_stages<L, 3>(x, p, m, kb, l, kb, tw);
-#pragma unroll
-                for (int h = 0; h < 8; ++h)
-                {
-#pragma unroll
-                    for (int j = 0; j < L; ++j)
-                    {
-                        p.out[static_cast<uint64_t>(j) * p.elements + base + (static_cast<uint64_t>(h) << kb) + l] =
-                            x[h][j];
-                    }
+                    p.out[static_cast<uint64_t>(j) * p.elements + e] = top[(g * 8u + h) * L + j];
                 }
             }
         }

@@ -432,8 +432,8 @@ namespace hmpc_gb300
             {
                 return configured;
             }
-            // one radix-8 group of the widest round per thread
-            const uint32_t work = 1u << (p.log_n - 6);
+            // one butterfly per thread and stage: N/16 per CTA
+            const uint32_t work = 1u << (p.log_n - 4);
             const unsigned threads = std::min(256u, std::max(32u, work));
             ntt_cluster_kernel<L><<<static_cast<unsigned>(batch * cl_ctas), threads, smem, stream>>>(p, device_modulus(h));
             return cudaGetLastError();
