@@ -617,62 +617,66 @@ namespace hmpc_gb300
         }
     }
 
-    // The signed value sum_j (x_j - 0x80808080) 2^(32 j) + top 2^(32 L) --
-    // x the carried digits packed as biased bytes, each word minus its bias in
-    // (-2^31, 2^32), |value / q| < 2^15 -- reduced into [0, q).  The quotient
-    // estimate reads the top word top * 2^32 + x[L-1] - 0x80808080 as one
-    // signed 64-bit integer converted once to f32 (relative error 2^-24: at
-    // most 2^-9 in the quotient) and scales it by 2^(32(L-1)) / q; the lower
-    // words, each in (-2^31, 2^32), move it by less than 1 / 32 either way for a
-    // top limb of q >= 32.  So t is within one of the quotient, the bias comes
-    // off in the same pass as t * q, and one correction each way -- both
-    // computed, then selected, so no lane branches -- gives the reduced value.
-    // (Converting x[L-1] to f32 on its own would round a word near 2^32 by up
-    // to 128 before a negative top cancels it: 128 / 32 quotients at the
-    // smallest top limb.)
+    // the signed value sum_j x_j 2^(32 j) + top 2^(32 L), |value / q| < 2^15,
+    // reduced into [0, q).  The quotient estimate reads the value's top word
+    // top * 2^32 + x[L-1] as one signed 64-bit integer converted once to f32
+    // (relative error 2^-24, so at most 2^-9 in the quotient), then scales by
+    // 2^(32(L-1)) / q; the dropped limbs add at most 1 / 32 for a top limb of
+    // q >= 32.  The estimate is within one of the quotient: one correction each
+    // way.  (Converting x[L-1] to f32 on its own would round a word near 2^32
+    // by up to 128 before a negative top cancels it -- 128 / 32 quotient units
+    // at the smallest top limb.)
     template<int L>
-    __device__ __forceinline__ void tc_reduce_biased(uint32_t (&x)[L], int top, const TcGroupParams& p)
+    __device__ __forceinline__ void tc_reduce(uint32_t (&x)[L], int top, const TcGroupParams& p)
     {
-        const long long top_word = static_cast<long long>(top) * 4294967296ll + static_cast<long long>(x[L - 1]) -
-                                   0x80808080ll;
+        const long long top_word = static_cast<long long>(top) * 4294967296ll + static_cast<long long>(x[L - 1]);
         const float est = static_cast<float>(top_word) * p.inv_q_top;
         const int t = __float2int_rd(est);
         long long carry = 0;
 #pragma unroll
         for (int j = 0; j < L; ++j)
         {
-            const long long acc = static_cast<long long>(x[j]) - 0x80808080ll - static_cast<long long>(t) * p.q[j] +
-                                  carry;
+            const long long acc = static_cast<long long>(x[j]) - static_cast<long long>(t) * p.q[j] + carry;
             x[j] = static_cast<uint32_t>(acc);
             carry = acc >> 32;
         }
-        // value - t q = x + rt 2^(32 L) with rt in {-1, 0, 1}: add q when
-        // negative, then subtract q when at least q
-        const int rt = top + static_cast<int>(carry);
-        const bool neg = rt < 0;
-        uint32_t c = 0;
-#pragma unroll
-        for (int j = 0; j < L; ++j)
+        int rt = top + static_cast<int>(carry);
+        if (rt < 0)
         {
-            const unsigned long long sum = static_cast<unsigned long long>(x[j]) + (neg ? p.q[j] : 0u) + c;
-            x[j] = static_cast<uint32_t>(sum);
-            c = static_cast<uint32_t>(sum >> 32);
+            uint32_t c = 0;
+#pragma unroll
+            for (int j = 0; j < L; ++j)
+            {
+                const unsigned long long s = static_cast<unsigned long long>(x[j]) + p.q[j] + c;
+                x[j] = static_cast<uint32_t>(s);
+                c = static_cast<uint32_t>(s >> 32);
+            }
+            rt += static_cast<int>(c);
         }
-        const int r2 = rt + static_cast<int>(c);  // 0 or 1 now
-        uint32_t y[L];
-        uint32_t b = 0;
-#pragma unroll
-        for (int j = 0; j < L; ++j)
+        bool ge = rt > 0;
+        if (!ge)
         {
-            const unsigned long long d = static_cast<unsigned long long>(x[j]) - p.q[j] - b;
-            y[j] = static_cast<uint32_t>(d);
-            b = static_cast<uint32_t>(d >> 63);
+            ge = true;  // x == q counts as >= q
+#pragma unroll
+            for (int j = L - 1; j >= 0; --j)
+            {
+                if (x[j] != p.q[j])
+                {
+                    ge = x[j] > p.q[j];
+                    break;
+                }
+            }
         }
-        const bool ge = r2 > 0 || b == 0;
-#pragma unroll
-        for (int j = 0; j < L; ++j)
+        if (ge)
         {
-            x[j] = ge ? y[j] : x[j];
+            uint32_t b = 0;
+#pragma unroll
+            for (int j = 0; j < L; ++j)
+            {
+                const unsigned long long s = static_cast<unsigned long long>(x[j]) - p.q[j] - b;
+                x[j] = static_cast<uint32_t>(s);
+                b = static_cast<uint32_t>(s >> 63);
+            }
         }
     }
 
@@ -756,12 +760,15 @@ namespace hmpc_gb300
             {
                 // value = (packed biased bytes) - 0x8080..80 + carry * 2^(8 DC)
                 uint32_t x[L];
+                uint32_t borrow = 0;
 #pragma unroll
                 for (int j = 0; j < L; ++j)
                 {
-                    x[j] = words[j];
+                    const unsigned long long d = static_cast<unsigned long long>(words[j]) - 0x80808080u - borrow;
+                    x[j] = static_cast<uint32_t>(d);
+                    borrow = static_cast<uint32_t>(d >> 63);
                 }
-                tc_reduce_biased<L>(x, carry.carry(), p);
+                tc_reduce<L>(x, carry.carry() - static_cast<int>(borrow), p);
 #pragma unroll
                 for (int j = 0; j < L; ++j)
                 {

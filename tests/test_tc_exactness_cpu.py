@@ -10,9 +10,9 @@ These restate three pieces of hmpc_gb300/csrc/tensor_ntt.cuh step by step:
 * DigitCarry (four operations per digit, groups fed by limbs): every
   intermediate an integer in [0, 2^24), with column sums of up to
   K * 255 * 128 (K = 8 elements x 4L bytes);
-* tc_reduce_biased: the quotient estimate from the value's signed top word
-  (carry and the top biased word) in f32 (times 2^(32(L-1)) / q rounded to
-  f32) leaves a remainder in [-q, 2q), so one correction each way
+* tc_reduce: the quotient estimate from the value's signed top word in f32
+  (times 2^(32(L-1)) / q rounded to f32) leaves a remainder in [-q, 2q), so
+  one correction each way
   gives the reduced representative, for |value / q| < 2^15 and q at both
   admission edges (top limb 32, floor(q/2) = 0x7F..7F).
 
@@ -103,28 +103,16 @@ def test_four_operation_carry_of_limb_input(limbs):
         assert value_of(digits, carry) == sum(s << (8 * j) for j, s in enumerate(sums))
 
 
-def biased_words(value, limbs):
-    """the last group's view of a value: its 4L balanced base-256 digits
-    packed as biased bytes (digit + 128) into L words, and the carry above
-    them (value = sum_j (w_j - 0x80808080) 2^(32 j) + carry 2^(32 L))"""
-    digits = []
-    v = value
-    for _ in range(4 * limbs):
-        d = ((v + 128) % 256) - 128
-        digits.append(d)
-        v = (v - d) // 256
-    words = [sum((digits[4 * j + i] + 128) << (8 * i) for i in range(4)) for j in range(limbs)]
-    assert sum((w - 0x80808080) << (32 * j) for j, w in enumerate(words)) + (v << (32 * limbs)) == value
-    return words, v
-
-
 def quotient_estimate(value, q, limbs):
-    """tc_reduce_biased's t: the top word carry * 2^32 + w_{L-1} - 0x80808080
-    as one 64-bit integer converted once to f32, times 2^(32(L-1)) / q in f32"""
+    """tc_reduce's t from the top word of the value (the carry out and limb
+    L-1), in f32 exactly as the device rounds"""
     top_d = (q >> (32 * (limbs - 1))) + ((q >> (32 * (limbs - 2))) & 0xFFFFFFFF) / 4294967296.0
     inv_q_top = np.float32(1.0 / top_d)
-    words, carry = biased_words(value, limbs)
-    word = carry * (1 << 32) + words[-1] - 0x80808080
+    u = value % (1 << (32 * limbs))  # limbs as stored (two's complement wrap)
+    top = value >> (32 * limbs)  # signed carry above the limbs
+    x_top = (u >> (32 * (limbs - 1))) & 0xFFFFFFFF
+    # the signed top word as one 64-bit integer, converted once to f32
+    word = top * (1 << 32) + x_top
     est = np.float32(np.float32(np.int64(word)) * inv_q_top)
     return int(np.floor(np.float64(est)))
 
