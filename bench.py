@@ -82,6 +82,46 @@ def rate_probes():
     return rates
 
 
+def pin_to_gpu_cpus(device_index):
+    """Run this process on the CPUs that nvidia-smi reports as local to the
+    GPU (its "CPU Affinity" in `nvidia-smi topo -m`), so that pinned host
+    buffers allocated afterwards sit on the GPU's NUMA node.  Returns what was
+    found and applied; changes nothing when the topology is not reported."""
+    import torch
+
+    info = {"applied": False}
+    try:
+        bus = torch.cuda.get_device_properties(device_index).pci_bus_id.lower()
+        ids = subprocess.run(["nvidia-smi", "--query-gpu=index,pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30).stdout
+        smi_index = None
+        for line in ids.splitlines():
+            idx, pci = [x.strip() for x in line.split(",")[:2]]
+            if pci.lower().endswith(bus[-12:]) or bus.endswith(pci.lower()[-12:]):
+                smi_index = int(idx)
+        topo = subprocess.run(["nvidia-smi", "topo", "-m"], capture_output=True, text=True, timeout=30).stdout
+        lines = [l for l in topo.splitlines() if l.strip()]
+        header = next(l for l in lines if "CPU Affinity" in l)
+        col = header.index("CPU Affinity")
+        row = next(l for l in lines if smi_index is not None and l.split()[0] == f"GPU{smi_index}")
+        field = row[col:].split()[0]
+        cpus = set()
+        for part in field.split(","):
+            if "-" in part:
+                a, b = part.split("-")
+                cpus.update(range(int(a), int(b) + 1))
+            elif part.isdigit():
+                cpus.add(int(part))
+        cpus &= set(os.sched_getaffinity(0))
+        info["gpu_cpus"] = field
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+            info["applied"] = True
+    except Exception as e:  # no topology report: leave the process where it is
+        info["error"] = type(e).__name__
+    return info
+
+
 def mont_mul_ops(limbs):
     """32-bit multiply operations of one L-limb Montgomery product:
     L^2 lo/hi product pairs plus L(L+1) reduction products (4L^2 + L)"""
@@ -913,6 +953,11 @@ def main():
     # copies of one step overlap the encryption of the next (a copy-in and a
     # copy-out stream, two buffer sets; events order the reuse of each set).
     copy_in, copy_out = torch.cuda.Stream(local), torch.cuda.Stream(local)
+    # pinned host buffers on the CPUs next to this GPU (the pages of a pinned
+    # allocation land on the NUMA node of the thread that allocates them); the
+    # process's CPU set is restored once they exist
+    cpu_set = os.sched_getaffinity(0)
+    host_numa = pin_to_gpu_cpus(local)
     host_msgs = torch.empty(msgs.data.shape, dtype=torch.int32, pin_memory=True)
     host_msgs.copy_(msgs.data.cpu())
     sets = []
@@ -927,6 +972,7 @@ def main():
     for b in sets:
         b["read"].record(stream)
         b["done"].record(stream)
+    os.sched_setaffinity(0, cpu_set)
 
     def e2e_step(i):
         b = sets[i % 2]
@@ -980,6 +1026,19 @@ def main():
         link[name] = 3 * src.numel() * 4 / (c_start.elapsed_time(c_stop) * 1e-3) / 1e9
     copy_s = max(host_msgs.numel() * 4 / (link["h2d"] * 1e9),
                  (host_c0.numel() + host_c1.numel()) * 4 / (link["d2h"] * 1e9))
+    # the same device-to-host copy while a step computes on the queue's
+    # stream: equal to the rate alone when copies and kernels overlap
+    c_start, c_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    step(msgs)
+    with torch.cuda.stream(copy_out):
+        c_start.record(copy_out)
+        for _ in range(3):
+            host_c0.copy_(sets[0]["ct"].c0.data, non_blocking=True)
+        c_stop.record(copy_out)
+    step(msgs)
+    barrier()
+    link["d2h_during_compute"] = 3 * host_c0.numel() * 4 / (c_start.elapsed_time(c_stop) * 1e-3) / 1e9
 
     # ------------------------------------------- dominant kernel roofline
     # the fused CBD(10) -> NTT over the batch: the transform's kernel launches
@@ -1022,6 +1081,7 @@ def main():
                 "decrypts_ok": ok,
                 "link_gbs": link,
                 "copy_bound": BATCH / copy_s,
+                "host_numa": host_numa,
             },
             "gpu_launches": launches,
             "roofline": roofline,
