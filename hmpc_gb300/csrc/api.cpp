@@ -3,7 +3,6 @@
 #include "../../include/hmpc_gb300.h"
 
 #include <algorithm>
-#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -52,12 +51,6 @@ namespace
     host::words to_words(const uint32_t* p, int n)
     {
         return host::words(p, p + n);
-    }
-
-    int enc_combine_chunks()
-    {
-        const char* v = std::getenv("HMPC_GB300_ENC_CHUNKS");
-        return v ? std::atoi(v) : 4;
     }
 }
 
@@ -1197,25 +1190,18 @@ int hmpc_lhe_enc(hmpc_context* ctx, hmpc_modulus* q, hmpc_modulus* p, uint64_t n
         parts[2].vx2 = 20;
         parts[2].small = &no_msg;
         uint32_t* stacked = ws;  // [L][3 * elements]: u | p*v + lift(m) | p*w, in NTT form
-        // The combine runs per chunk of coefficients as soon as the last
-        // group has finished them, one block per SM beside the next chunk's
-        // group (whose CTAs are latency-bound and leave room for it).
-        TcChunkSink combine;
-        combine.chunks = enc_combine_chunks();
-        combine.run = [&](uint64_t lo, uint32_t log_count, cudaStream_t stream, bool beside) -> int {
-            const unsigned grid = beside ? static_cast<unsigned>(ctx->sm_count) : 0u;
-            cudaError_t e = q->kt->lhe_combine_pair(c0, c1, key_a, key_b, n, stacked, elements, lo, log_count, grid,
-                                                    q->h, stream);
+        if (!rc)
+        {
+            rc = run_tc_stacked(ctx, q, n, batch, parts, 3, stacked, tc_splits);
+        }
+        if (!rc)
+        {
+            cudaError_t e = q->kt->lhe_combine_pair(c0, c1, key_a, key_b, n, stacked, elements, q->h, ctx->stream);
             if (e != cudaSuccess)
             {
                 return cuda_fail(e, "launching combine");
             }
             ++ctx->launches;
-            return HMPC_OK;
-        };
-        if (!rc)
-        {
-            rc = run_tc_stacked(ctx, q, n, batch, parts, 3, stacked, tc_splits, &combine);
         }
         return rc;
     }

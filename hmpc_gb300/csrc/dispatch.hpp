@@ -80,9 +80,8 @@ namespace hmpc_gb300
         int (*ntt_batched_blocks_per_sm)(int radix_bits, size_t smem);
         int radix_bits;
         cudaError_t (*lhe_combine_pair)(uint32_t* c0, uint32_t* c1, const uint32_t* ka, const uint32_t* kb,
-                                        uint64_t n, const uint32_t* stacked, uint64_t elements, uint64_t lo,
-                                        uint32_t log_count, unsigned grid, const HostModulus& m,
-                                        cudaStream_t stream);
+                                        uint64_t n, const uint32_t* stacked, uint64_t elements,
+                                        const HostModulus& m, cudaStream_t stream);
         // matrix-vector products (linalg.cuh)
         cudaError_t (*matvec)(uint32_t* z, const uint32_t* mat, const uint32_t* x, const MatvecParams& p,
                               const HostModulus& m, cudaStream_t stream);

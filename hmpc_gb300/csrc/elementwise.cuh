@@ -173,33 +173,28 @@ namespace hmpc_gb300
     // p * w already went through the transform as inputs of their own
     // (linearity of the NTT).  u, x, w are the three parts of one stacked
     // transform output, [L][3 * elements]; u is read once for both products.
-    // One element per thread (64 registers at L = 8): enough resident warps
-    // to cover the loads' latency with the products' arithmetic.  The call
-    // covers the coefficients [lo, lo + 2^log_count) of every polynomial
-    // (all of them: lo = 0, 2^log_count = n); n is a power of two.
+    // One element per thread (about 50 registers at L = 8): enough resident
+    // warps to cover the loads' latency with the products' arithmetic.
+    // n is a power of two.
     template<int L>
     __global__ void __launch_bounds__(256) lhe_combine_pair_kernel(uint32_t* c0, uint32_t* c1, const uint32_t* ka,
                                                                    const uint32_t* kb, uint64_t n,
                                                                    const uint32_t* stacked, uint64_t elements,
-                                                                   uint64_t lo, uint32_t log_count,
                                                                    const Modulus<L> m)
     {
         const uint64_t stride = 3 * elements;
-        const uint64_t count_mask = (1ull << log_count) - 1;
-        const uint64_t work = elements / n << log_count;
-        for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < work;
-             t += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        const uint64_t mask = n - 1;
+        for (uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < elements;
+             e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
         {
-            const uint64_t c = lo + (t & count_mask);
-            const uint64_t e = (t >> log_count) * n + c;
             uint32_t u[L], k[L], x[L];
             load1<L>(u, stacked, stride, e);
-            load1<L>(k, ka, n, c);
+            load1<L>(k, ka, n, e & mask);
             load1<L>(x, stacked + elements, stride, e);
             mont_mul<L>(k, k, u, m);
             mod_add<L>(x, x, k, m);
             store1<L>(c0, elements, e, x);
-            load1<L>(k, kb, n, c);
+            load1<L>(k, kb, n, e & mask);
             load1<L>(x, stacked + 2 * elements, stride, e);
             mont_mul<L>(k, k, u, m);
             mod_add<L>(x, x, k, m);

@@ -5,7 +5,6 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
-#include <functional>
 #include <mutex>
 #include <tuple>
 #include <string>
@@ -292,19 +291,8 @@ namespace hmpc_gb300::detail
         uint32_t vx2 = 0;
         const TcSmallInput* small = nullptr;  // nullptr: plain CBD(V) input
     };
-    // Work on finished coefficients: with a sink, the last group runs as
-    // `chunks` launches over consecutive ranges of its blocks, and after each
-    // one `run` is called for the coefficients [lo, lo + 2^log_count) of every
-    // polynomial, on `stream` (the context's second stream when chunks > 1,
-    // where `beside` says the next chunk's transform runs at the same time).
-    // The context stream waits for all of it before the call returns.
-    struct TcChunkSink
-    {
-        int chunks = 1;
-        std::function<int(uint64_t lo, uint32_t log_count, cudaStream_t stream, bool beside)> run;
-    };
     int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
-                       int count, uint32_t* out, int splits, const TcChunkSink* sink = nullptr);
+                       int count, uint32_t* out, int splits);
     int tc_cost(hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind, int splits, hmpc_tc_cost* out);
     // Polynomials of one degree n in buffers of their own (the batched
     // transform's buckets).  tc_prepare_polys builds the constants of (n,

@@ -351,27 +351,16 @@ namespace hmpc_gb300
             return e == cudaSuccess ? blocks : 0;
         }
 
-        // grid 0: sized by the work; else that many blocks (one per SM leaves
-        // room beside a tensor-core group's CTA).  Kept on the shared-memory
-        // carveout the group kernels run with, so its blocks never hold an SM
-        // in another configuration.
         cudaError_t lhe_combine_pair(uint32_t* c0, uint32_t* c1, const uint32_t* ka, const uint32_t* kb, uint64_t n,
-                                     const uint32_t* stacked, uint64_t elements, uint64_t lo, uint32_t log_count,
-                                     unsigned grid, const HostModulus& h, cudaStream_t stream)
+                                     const uint32_t* stacked, uint64_t elements, const HostModulus& h,
+                                     cudaStream_t stream)
         {
             if (elements == 0)
             {
                 return cudaSuccess;
             }
-            static const cudaError_t carveout = cudaFuncSetAttribute(
-                lhe_combine_pair_kernel<L>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-            if (carveout != cudaSuccess)
-            {
-                return carveout;
-            }
-            const uint64_t work = elements / n << log_count;
-            lhe_combine_pair_kernel<L><<<grid ? grid : grid_for(work, 256), 256, 0, stream>>>(
-                c0, c1, ka, kb, n, stacked, elements, lo, log_count, device_modulus(h));
+            lhe_combine_pair_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(c0, c1, ka, kb, n, stacked,
+                                                                                   elements, device_modulus(h));
             return cudaGetLastError();
         }
 

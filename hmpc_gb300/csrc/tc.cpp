@@ -369,10 +369,8 @@ namespace hmpc_gb300::detail
         }
 
         // group j over `batch` polynomials; stride = plane stride of the digit / limb planes
-        // blocks [block_lo, block_lo + block_count) of the group (block_count 0: all)
         int group(size_t j, const uint32_t* in, uint32_t* out, uint64_t stride, uint64_t batch, int in_kind,
-                  uint32_t vx2, const TcSmallInput* small, uint64_t msg_stride, uint64_t block_lo = 0,
-                  uint64_t block_count = 0)
+                  uint32_t vx2, const TcSmallInput* small, uint64_t msg_stride)
         {
             const TcGroupPlan& gp = tt->groups[j];
             const bool first_sampled = j == 0 && (in_kind == tc_in_cbd || in_kind == tc_in_small);
@@ -385,9 +383,7 @@ namespace hmpc_gb300::detail
             p.elements = stride;
             p.rows = batch << gp.lo;
             p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
-            const uint64_t tiles_per_hb = gp.shape.splits * p.tiles_per_block;
-            p.tiles = (block_count ? block_count : gp.blocks) * tiles_per_hb;
-            p.tile_base = block_lo * tiles_per_hb;
+            p.tiles = gp.blocks * gp.shape.splits * p.tiles_per_block;
             p.log_n = log_n;
             p.lo = gp.lo;
             p.spin_limit = ctx->tc_spin_limit;
@@ -495,7 +491,7 @@ namespace hmpc_gb300::detail
     }
 
     int run_tc_stacked(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, const TcStackPart* parts,
-                       int count, uint32_t* out, int splits, const TcChunkSink* sink)
+                       int count, uint32_t* out, int splits)
     {
         bool need_cbd = false, need_small = false;
         for (int i = 0; i < count; ++i)
@@ -548,72 +544,15 @@ namespace hmpc_gb300::detail
             nonce_add(ctx->nonce, elements);
         }
         // the shared groups over the stacked batch
-        const uint64_t rows = batch * static_cast<uint64_t>(count);
-        for (size_t j = 1; j + 1 < stages; ++j)
+        for (size_t j = 1; j < stages; ++j)
         {
             const uint32_t* in = digits + (((j - 1) & 1u) ? w * total : 0);
-            uint32_t* o = digits + ((j & 1u) ? w * total : 0);
-            if (int rc = run.group(j, in, o, total, rows, tc_in_digits, 0, nullptr, 0))
+            uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * total : 0);
+            if (int rc = run.group(j, in, o, total, batch * static_cast<uint64_t>(count), tc_in_digits, 0, nullptr, 0))
             {
                 return rc;
             }
         }
-        const uint32_t* last_in = stages == 1 ? nullptr : digits + (((stages - 2) & 1u) ? w * total : 0);
-        const uint32_t log_n = static_cast<uint32_t>(__builtin_ctzll(n));
-        if (stages == 1 || !sink)
-        {
-            if (stages > 1)
-            {
-                if (int rc = run.group(stages - 1, last_in, out, total, rows, tc_in_digits, 0, nullptr, 0))
-                {
-                    return rc;
-                }
-            }
-            return sink ? sink->run(0, log_n, ctx->stream, false) : HMPC_OK;
-        }
-        // The last group always holds the transform's final stage, so its
-        // block h covers the adjacent coefficients [h * r, (h + 1) * r) of
-        // every polynomial: a range of blocks is a range of coefficients.
-        // Chunks run on the context stream one after the other; the sink's
-        // work on chunk c runs on the second stream beside chunk c + 1.  Each
-        // chunk keeps every SM busy for at least four tiles.
-        const TcGroupPlan& last = tt->groups.back();
-        const uint64_t tiles_per_block = last.shape.splits * (((rows << last.lo) + tc_rows - 1) / tc_rows);
-        uint64_t chunks = sink->chunks > 1 ? static_cast<uint64_t>(sink->chunks) : 1;
-        while (chunks > 1 && (last.blocks % chunks != 0 ||
-                              last.blocks / chunks * tiles_per_block < 4ull * static_cast<uint64_t>(ctx->sm_count)))
-        {
-            chunks >>= 1;
-        }
-        if (chunks == 1)
-        {
-            if (int rc = run.group(stages - 1, last_in, out, total, rows, tc_in_digits, 0, nullptr, 0))
-            {
-                return rc;
-            }
-            return sink->run(0, log_n, ctx->stream, false);
-        }
-        if (!ctx->aux())
-        {
-            return fail(HMPC_ERROR_CUDA, "creating the second stream");
-        }
-        const uint64_t per = last.blocks / chunks;
-        const uint32_t log_count = static_cast<uint32_t>(__builtin_ctzll(per)) + static_cast<uint32_t>(last.g);
-        for (uint64_t c = 0; c < chunks; ++c)
-        {
-            if (int rc = run.group(stages - 1, last_in, out, total, rows, tc_in_digits, 0, nullptr, 0, c * per, per))
-            {
-                return rc;
-            }
-            HMPC_CUDA(cudaEventRecord(ctx->fork_event, ctx->stream), "ordering a chunk's follow-up work");
-            HMPC_CUDA(cudaStreamWaitEvent(ctx->aux_stream, ctx->fork_event, 0), "ordering a chunk's follow-up work");
-            if (int rc = sink->run((c * per) << last.g, log_count, ctx->aux_stream, c + 1 < chunks))
-            {
-                return rc;
-            }
-        }
-        HMPC_CUDA(cudaEventRecord(ctx->join_event, ctx->aux_stream), "joining the chunks' follow-up work");
-        HMPC_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join_event, 0), "joining the chunks' follow-up work");
         return HMPC_OK;
     }
 

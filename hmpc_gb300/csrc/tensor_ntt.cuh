@@ -81,8 +81,7 @@ namespace hmpc_gb300
         uint32_t* error;           // set when a bounded wait runs out
         uint64_t elements;         // batch * N
         uint64_t rows;             // rows per block: batch << lo
-        uint64_t tiles;            // tiles of this launch (all: blocks * NS * tiles_per_block)
-        uint64_t tile_base;        // first tile of this launch (a launch over a range of blocks)
+        uint64_t tiles;            // blocks * NS * tiles_per_block
         uint32_t tiles_per_block;
         uint32_t log_n;
         uint32_t lo;               // column bits below the group's element bits
@@ -865,8 +864,8 @@ namespace hmpc_gb300
         const uint32_t tid = threadIdx.x;
         const uint32_t warp = tid >> 5, lane = tid & 31u;
 
-        const uint64_t t_begin = p.tile_base + p.tiles * blockIdx.x / gridDim.x;
-        const uint64_t t_end = p.tile_base + p.tiles * (blockIdx.x + 1) / gridDim.x;
+        const uint64_t t_begin = p.tiles * blockIdx.x / gridDim.x;
+        const uint64_t t_end = p.tiles * (blockIdx.x + 1) / gridDim.x;
         const uint64_t count = t_end - t_begin;
         const uint32_t tpb = p.tiles_per_block;
         const uint64_t hb_first = t_begin / tpb;
