@@ -51,15 +51,13 @@ def test_three_transform_encryption_matches_oracle(queue, oracle, qv, pv, n, bat
     ct = lhe.enc(queue, key, msgs, gq, plaintext_ntt=plaintext_ntt)
     groups = (n.bit_length() - 1 + 2) // 3
     # u, p*v + lift(m) and p*w stacked on the tensor cores (three first-group
-    # launches, then one launch per middle group), the last group in 1, 2 or 4
-    # chunks of coefficients with one combine writing c0 and c1 per chunk
-    # (more chunks only where each keeps every SM busy for four tiles), and the
-    # INTT mod p when the plaintext is in NTT form
+    # launches, then one launch per remaining group), one combine writing c0
+    # and c1, and the INTT mod p when the plaintext is in NTT form
     launched = queue.launches - before
     if plaintext_ntt:
-        assert launched > 3 + (groups - 2) + 2
+        assert launched > 3 + (groups - 1) + 1
     else:
-        assert launched - (3 + (groups - 2)) in (2, 4, 8)
+        assert launched == 3 + (groups - 1) + 1
     c0, c1, nonce_ref = oracle.lhe_enc(om_q, om_p, n, batch, a_ref, b_ref, msgs_ref, plaintext_ntt, KEY, nonce,
                                        threads=cpu_threads)
     assert queue.nonce == nonce_ref
