@@ -91,13 +91,15 @@ def pin_to_gpu_cpus(device_index):
 
     info = {"applied": False}
     try:
-        bus = torch.cuda.get_device_properties(device_index).pci_bus_id.lower()
+        props = torch.cuda.get_device_properties(device_index)
+        want = (int(props.pci_domain_id), int(props.pci_bus_id), int(props.pci_device_id))
         ids = subprocess.run(["nvidia-smi", "--query-gpu=index,pci.bus_id", "--format=csv,noheader"],
                              capture_output=True, text=True, timeout=30).stdout
         smi_index = None
         for line in ids.splitlines():
             idx, pci = [x.strip() for x in line.split(",")[:2]]
-            if pci.lower().endswith(bus[-12:]) or bus.endswith(pci.lower()[-12:]):
+            domain, bus, devfn = pci.split(":")  # e.g. 00000009:01:00.0
+            if (int(domain, 16), int(bus, 16), int(devfn.split(".")[0], 16)) == want:
                 smi_index = int(idx)
         topo = subprocess.run(["nvidia-smi", "topo", "-m"], capture_output=True, text=True, timeout=30).stdout
         lines = [l for l in topo.splitlines() if l.strip()]
