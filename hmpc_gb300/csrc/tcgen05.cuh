@@ -214,17 +214,4 @@ namespace hmpc_gb300::tc
     {
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     }
-
-    // the wait, with the registers of the load it completes passed through
-    // an empty statement after it: their readers cannot move above the wait
-    template<int N>
-    __device__ __forceinline__ void tmem_load_wait(uint32_t (&r)[N])
-    {
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-        for (int i = 0; i < N; ++i)
-        {
-            asm volatile("" : "+r"(r[i]));
-        }
-    }
 }

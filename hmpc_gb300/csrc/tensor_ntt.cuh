@@ -680,37 +680,6 @@ namespace hmpc_gb300
         }
     }
 
-    // The value sum_b s_b 256^b of 4L exact f32 column sums with every
-    // |s_b| < 2^22 (groups fed by digits: at most 128 * 32512), as L 32-bit
-    // words and a signed top word (out[L], two's complement).  s + 1.5 * 2^23
-    // is a float in [2^23, 2^24) whose bits are 0x4B400000 + s, so four sums
-    // combine into one 64-bit word of the value (plus the constant bias
-    // 0x4B400000 * 0x01010101), and a single carry chain over L words
-    // replaces the carry from digit to digit: the words are independent and
-    // the dependent chain is L long instead of 4L.
-    template<int L>
-    __device__ __forceinline__ void tc_sums_to_limbs(const uint32_t (&s)[4 * L], uint32_t* out)
-    {
-        constexpr long long bias = 0x4B400000ll * 0x01010101ll;
-        long long carry = 0;
-#pragma unroll
-        for (int j = 0; j < L; ++j)
-        {
-            const uint32_t b0 = __float_as_uint(__fadd_rn(__uint_as_float(s[4 * j]), 12582912.0f));
-            const uint32_t b1 = __float_as_uint(__fadd_rn(__uint_as_float(s[4 * j + 1]), 12582912.0f));
-            const uint32_t b2 = __float_as_uint(__fadd_rn(__uint_as_float(s[4 * j + 2]), 12582912.0f));
-            const uint32_t b3 = __float_as_uint(__fadd_rn(__uint_as_float(s[4 * j + 3]), 12582912.0f));
-            const unsigned long long w = static_cast<unsigned long long>(b0) +
-                                         (static_cast<unsigned long long>(b1) << 8) +
-                                         (static_cast<unsigned long long>(b2) << 16) +
-                                         (static_cast<unsigned long long>(b3) << 24);
-            const long long acc = static_cast<long long>(w) - bias + carry;
-            out[j] = static_cast<uint32_t>(acc);
-            carry = acc >> 32;
-        }
-        out[L] = static_cast<uint32_t>(carry);
-    }
-
     template<int Per>
     __device__ __forceinline__ void store_run(uint32_t* p, const uint32_t (&v)[Per])
     {
@@ -763,76 +732,47 @@ namespace hmpc_gb300
             op = r.ok ? p.out_polys[r.poly] + (r.base & (ostride - 1ull)) : p.out;
         }
         uint32_t res[Contig ? words_out : 1][Contig ? per : 1];
-        // Contig (one CTA of 9 warps per SM, registers to spare): the next
-        // element's sums load from TMEM while this one is carried
-        constexpr bool ahead = Contig && per > 1;
-        const uint32_t taddr = tmem + ((32u * lg) << 16) + kl0 * DC;
-        uint32_t sums[ahead ? 2 : 1][DC];
-        if constexpr (ahead)
-        {
-            tc_load_sums<DC>(taddr, sums[0]);
-        }
 #pragma unroll
         for (int kk = 0; kk < per; ++kk)
         {
-            uint32_t(&s)[DC] = sums[ahead ? (kk & 1) : 0];
-            if constexpr (ahead)
-            {
-                tc::tmem_load_wait(s);
-                if (kk + 1 < per)
-                {
-                    tc_load_sums<DC>(taddr + (kk + 1) * DC, sums[(kk + 1) & 1]);
-                }
-            }
-            else
-            {
-                tc_load_sums<DC>(taddr + kk * DC, s);
-                tc::tmem_load_wait(s);
-            }
+            uint32_t s[DC];
+            tc_load_sums<DC>(tmem + ((32u * lg) << 16) + (kl0 + kk) * DC, s);
+            tc::tmem_load_wait();
+            std::conditional_t<ByteCarry, DigitCarryByte, DigitCarry> carry;
             uint32_t words[W];
-            if constexpr (OUT == tc_out_limbs && ByteCarry)
+            uint32_t bb[4];
+#pragma unroll
+            for (int b = 0; b < DC; ++b)
             {
-                tc_sums_to_limbs<L>(s, words);
-                tc_reduce<L>(*reinterpret_cast<uint32_t(*)[L]>(&words[0]), static_cast<int>(words[L]), p);
+                bb[b & 3] = carry.step(__uint_as_float(s[b]));
+                if ((b & 3) == 3)
+                {
+                    words[b >> 2] = pack_bytes(bb[0], bb[1], bb[2], bb[3]);
+                }
+            }
+            if constexpr (OUT == tc_out_digits)
+            {
+                const uint32_t c0 = carry.step(0.0f);
+                const uint32_t c1 = carry.step(0.0f);
+                words[DC / 4] = pack_bytes(c0, c1, 0x80u, 0x80u);
             }
             else
             {
-                std::conditional_t<ByteCarry, DigitCarryByte, DigitCarry> carry;
-                uint32_t bb[4];
+                // value = (packed biased bytes) - 0x8080..80 + carry * 2^(8 DC)
+                uint32_t x[L];
+                uint32_t borrow = 0;
 #pragma unroll
-                for (int b = 0; b < DC; ++b)
+                for (int j = 0; j < L; ++j)
                 {
-                    bb[b & 3] = carry.step(__uint_as_float(s[b]));
-                    if ((b & 3) == 3)
-                    {
-                        words[b >> 2] = pack_bytes(bb[0], bb[1], bb[2], bb[3]);
-                    }
+                    const unsigned long long d = static_cast<unsigned long long>(words[j]) - 0x80808080u - borrow;
+                    x[j] = static_cast<uint32_t>(d);
+                    borrow = static_cast<uint32_t>(d >> 63);
                 }
-                if constexpr (OUT == tc_out_digits)
-                {
-                    const uint32_t c0 = carry.step(0.0f);
-                    const uint32_t c1 = carry.step(0.0f);
-                    words[DC / 4] = pack_bytes(c0, c1, 0x80u, 0x80u);
-                }
-                else
-                {
-                    // value = (packed biased bytes) - 0x8080..80 + carry * 2^(8 DC)
-                    uint32_t x[L];
-                    uint32_t borrow = 0;
+                tc_reduce<L>(x, carry.carry() - static_cast<int>(borrow), p);
 #pragma unroll
-                    for (int j = 0; j < L; ++j)
-                    {
-                        const unsigned long long d =
-                            static_cast<unsigned long long>(words[j]) - 0x80808080u - borrow;
-                        x[j] = static_cast<uint32_t>(d);
-                        borrow = static_cast<uint32_t>(d >> 63);
-                    }
-                    tc_reduce<L>(x, carry.carry() - static_cast<int>(borrow), p);
-#pragma unroll
-                    for (int j = 0; j < L; ++j)
-                    {
-                        words[j] = x[j];
-                    }
+                for (int j = 0; j < L; ++j)
+                {
+                    words[j] = x[j];
                 }
             }
             if constexpr (Contig)

@@ -10,9 +10,6 @@ These restate three pieces of hmpc_gb300/csrc/tensor_ntt.cuh step by step:
 * DigitCarry (four operations per digit, groups fed by limbs): every
   intermediate an integer in [0, 2^24), with column sums of up to
   K * 255 * 128 (K = 8 elements x 4L bytes);
-* tc_sums_to_limbs (the last group's column sums straight to limbs): every
-  s + 1.5 * 2^23 must lie in [2^23, 2^24), where the float's bits are
-  0x4B400000 + s, and the 64-bit word sums and carries must equal the value;
 * tc_reduce: the quotient estimate from the value's signed top word in f32
   (times 2^(32(L-1)) / q rounded to f32) leaves a remainder in [-q, 2q), so
   one correction each way
@@ -104,48 +101,6 @@ def test_four_operation_carry_of_limb_input(limbs):
     for sums in seqs:
         digits, carry = four_op_carry(sums)
         assert value_of(digits, carry) == sum(s << (8 * j) for j, s in enumerate(sums))
-
-
-def sums_to_limbs(sums):
-    """tc_sums_to_limbs: L words (two's complement wrap) and the signed top"""
-    bias = 0x4B400000 * 0x01010101
-    carry = 0
-    words = []
-    for j in range(len(sums) // 4):
-        bits = []
-        for s in sums[4 * j:4 * j + 4]:
-            t = s + 12582912  # FADD: 1.5 * 2^23
-            assert TWO23 <= t < TWO24, t
-            bits.append(0x4B000000 + (t - TWO23))  # the float's bits
-        w = bits[0] + (bits[1] << 8) + (bits[2] << 16) + (bits[3] << 24)
-        assert 0 <= w < 1 << 64  # unsigned 64-bit word sum
-        acc = w - bias + carry
-        assert -(1 << 63) <= acc < 1 << 63  # signed 64-bit
-        words.append(acc & 0xFFFFFFFF)
-        carry = acc >> 32  # arithmetic shift
-    assert -(1 << 31) <= carry < 1 << 31
-    return words, carry
-
-
-@pytest.mark.parametrize("limbs", [2, 3, 4, 5, 6, 7, 8])
-def test_sums_to_limbs_at_the_column_bound(limbs):
-    limit = 128 * 32512
-    rng = np.random.default_rng(100 + limbs)
-    for sums in extreme_sequences(limit, 4 * limbs, rng):
-        words, top = sums_to_limbs(sums)
-        value = sum(w << (32 * j) for j, w in enumerate(words)) + (top << (32 * limbs))
-        assert value == sum(s << (8 * b) for b, s in enumerate(sums))
-        # the same value the digit-by-digit carry gives
-        digits, carry = byte_carry(sums)
-        assert value == value_of(digits, carry)
-
-
-def test_sums_to_limbs_needs_the_bound():
-    """a sum of 2^22 leaves the float range where the bits are the integer"""
-    with pytest.raises(AssertionError):
-        sums_to_limbs([1 << 22] + [0] * 31)
-    with pytest.raises(AssertionError):
-        sums_to_limbs([-(1 << 22) - 1] + [0] * 31)
 
 
 def quotient_estimate(value, q, limbs):
