@@ -154,9 +154,29 @@ namespace hmpc_gb300::detail
         if (choice.radix_bits == 0)
         {
             // tensor-core engine; calls it does not cover run the default CUDA-core tiles
-            if (!cuda_cores_only && tc_applicable(mod, log_n, kind, poly_rng))
+            if (!cuda_cores_only && tc_applicable(mod, log_n, kind, poly_rng) &&
+                (kind != producer_uniform || !inverse))
             {
-                return run_tc_transform(ctx, mod, n, batch, inverse, kind, vx2, src, out, choice.local_bits);
+                if (kind != producer_uniform)
+                {
+                    return run_tc_transform(ctx, mod, n, batch, inverse, kind, vx2, src, out, choice.local_bits);
+                }
+                // the engine's first group reads memory: the stage-0 pairs'
+                // uniform draws go to `out` first, then the transform runs in place
+                cudaError_t e = mod->kt->uniform_pairs(out, static_cast<uint32_t>(log_n), n * batch, ctx->rng(), nw,
+                                                       top_mask, mod->h, ctx->stream);
+                if (e != cudaSuccess)
+                {
+                    return cuda_fail(e, "launching the uniform pair sampler");
+                }
+                ++ctx->launches;
+                if (int rc = run_tc_transform(ctx, mod, n, batch, false, producer_tensor, 0, out, out,
+                                              choice.local_bits))
+                {
+                    return rc;
+                }
+                nonce_add(ctx->nonce, n * batch);
+                return HMPC_OK;
             }
             choice = hmpc_modulus::TileChoice{};
         }

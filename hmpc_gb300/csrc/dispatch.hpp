@@ -95,6 +95,10 @@ namespace hmpc_gb300
         // one thread-block cluster per polynomial (cluster.cuh), degrees 2^10..2^14
         cudaError_t (*ntt_cluster)(const ClusterNttParams& p, uint64_t batch, const HostModulus& m,
                                    cudaStream_t stream);
+        // the uniform draws of a forward transform's stage-0 pairs as its input
+        // (for the tensor-core engine, whose first group reads memory)
+        cudaError_t (*uniform_pairs)(uint32_t* out, uint32_t log_n, uint64_t elements, const RngKey& rng,
+                                     int words, uint32_t top_mask, const HostModulus& m, cudaStream_t stream);
     };
 
     // sizes of one tensor-core group kernel instantiation (TcShape)

@@ -276,6 +276,32 @@ namespace hmpc_gb300
         }
     }
 
+    // The uniform draws of a forward transform's stage-0 pairs, written as the
+    // transform's input: pair (j, j + n/2) of polynomial i uses the generator
+    // (key, nonce, counter = i * n + j) and draws element j's value, then
+    // element j + n/2's -- the values the sampler fused into the transform's
+    // first stage draws (expr/number_theoretic_transform.hpp:316-329), for a
+    // transform engine that reads its input from memory.  W words per value.
+    template<int L, int W>
+    __global__ void __launch_bounds__(256) uniform_pairs_kernel(uint32_t* out, uint32_t log_n, uint64_t elements,
+                                                                const RngKey rng, uint32_t top_mask,
+                                                                const Modulus<L> m)
+    {
+        const uint64_t half = 1ull << (log_n - 1);
+        for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < elements / 2;
+             t += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        {
+            const uint64_t e = ((t >> (log_n - 1)) << log_n) + (t & (half - 1));
+            uint32_t w[2 * W];
+            chacha_stream<2 * W>(rng, static_cast<uint32_t>(e), w);
+            uint32_t u[L], v[L];
+            uniform_from_words<L, W, 0, 2 * W>(u, w, top_mask, m);
+            uniform_from_words<L, W, W, 2 * W>(v, w, top_mask, m);
+            store1<L>(out, elements, e, u);
+            store1<L>(out, elements, e + half, v);
+        }
+    }
+
     template<int L, int NW>
     __global__ void __launch_bounds__(256) cbd_kernel(uint32_t* out, uint64_t elements, const RngKey rng,
                                                       uint32_t vx2, const uint32_t* small_table, const Modulus<L> m)

@@ -190,6 +190,31 @@ namespace hmpc_gb300
             return cudaGetLastError();
         }
 
+        cudaError_t uniform_pairs(uint32_t* out, uint32_t log_n, uint64_t elements, const RngKey& rng, int words,
+                                  uint32_t top_mask, const HostModulus& h, cudaStream_t stream)
+        {
+            if (elements < 2 || log_n < 1)
+            {
+                return elements ? cudaErrorInvalidValue : cudaSuccess;
+            }
+            const unsigned grid = grid_for(elements / 2, 256);
+            if (words == L + 2)
+            {
+                uniform_pairs_kernel<L, L + 2><<<grid, 256, 0, stream>>>(out, log_n, elements, rng, top_mask,
+                                                                         device_modulus(h));
+            }
+            else if (words == L + 3)
+            {
+                uniform_pairs_kernel<L, L + 3><<<grid, 256, 0, stream>>>(out, log_n, elements, rng, top_mask,
+                                                                         device_modulus(h));
+            }
+            else
+            {
+                return cudaErrorInvalidValue;
+            }
+            return cudaGetLastError();
+        }
+
         cudaError_t cbd(uint32_t* out, uint64_t elements, const RngKey& rng, uint32_t vx2, const uint32_t* table,
                         const HostModulus& h, cudaStream_t stream)
         {
@@ -442,7 +467,7 @@ namespace hmpc_gb300
         const KernelTable table = {ntt_pass, fma, binary, lhe_combine, uniform, cbd, to_montgomery,
                                    from_montgomery, cast, plain_stage, ct_mul, dec_combine, ntt_batched,
                                    ntt_batched_blocks_per_sm, R, lhe_combine_pair, matvec, matvec_monomial,
-                                   reduce, equal, ntt_cluster};
+                                   reduce, equal, ntt_cluster, uniform_pairs};
     }
 
     const KernelTable* HMPC_CAT(kernel_table_, HMPC_L)()

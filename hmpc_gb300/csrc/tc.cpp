@@ -324,7 +324,8 @@ namespace hmpc_gb300::detail
 
     bool tc_applicable(const hmpc_modulus* mod, int log_n, int kind, const uint32_t* poly_rng)
     {
-        return log_n >= 4 && !poly_rng && (kind == producer_tensor || kind == producer_cbd) && tc_supported(mod);
+        return log_n >= 4 && !poly_rng && (kind == producer_tensor || kind == producer_cbd || kind == producer_uniform) &&
+               tc_supported(mod);
     }
 
     // launch state shared by the groups of one transform (or one stack of them)

@@ -1,7 +1,7 @@
 """Parity of the tensor-core transform engine (tile shape radix bits 0) with
 the CPU oracle for moduli of 2 to 8 limbs: bit-exact forward and inverse transforms, fused CBD(V)
-samplers, ragged batches, in-place calls, and the fallback to the CUDA-core
-tiles for calls the engine does not cover."""
+samplers, the uniform sampler's transform, ragged batches, in-place calls, and
+the fallback to the CUDA-core tiles for calls the engine does not cover."""
 import numpy as np
 import pytest
 
@@ -137,15 +137,29 @@ def test_in_place_and_zero(queue, oracle):
     assert not queue.ntt(zero).numpy().any()
 
 
+@pytest.mark.parametrize("q", [Q_256, Q_128, Q_192, P_64, Q_96])
+@pytest.mark.parametrize("n,batch", [(16, 3), (1 << 10, 2), (1 << 12, 130)])
+def test_uniform_producer_on_the_engine(queue, oracle, q, n, batch, cpu_threads):
+    """the uniform sampler's transform: one launch draws the stage-0 pairs'
+    values (the generator of pair (j, j + n/2) at counter j, u before v)
+    into the output, then the engine's groups run in place"""
+    om, gm = oracle.Modulus(q), queue.modulus(q)
+    tensor_plan(gm, n, batch)
+    nonce = [0xFFFFFFF8, 3, 9]
+    queue.nonce = nonce
+    before = queue.launches
+    y = queue.ntt_uniform(gm, n, (batch,))
+    assert queue.launches - before == 1 + groups(n)
+    assert queue.nonce == oracle.nonce_add(nonce, n * batch)
+    ref = oracle.ntt(om, n, batch, sampler="uniform", key=KEY, nonce=nonce, threads=cpu_threads)
+    assert np.array_equal(y.numpy(), ref)
+
+
 def test_uncovered_calls_fall_back(queue, oracle):
-    """uniform samplers, degrees below 16 and unsupported moduli run the CUDA-core tiles"""
+    """degrees below 16 and unsupported moduli run the CUDA-core tiles"""
     gm = queue.modulus(Q_256)
     om = oracle.Modulus(Q_256)
     n, batch = 1 << 10, 2
-    tensor_plan(gm, n, batch)
-    queue.nonce = [1, 2, 3]
-    y = queue.ntt_uniform(gm, n, (batch,))
-    assert np.array_equal(y.numpy(), oracle.ntt(om, n, batch, sampler="uniform", key=KEY, nonce=[1, 2, 3]))
     g288 = queue.modulus(Q_288)
     with pytest.raises(_lib.HmpcError):
         g288.set_plan(n, batch, False, radix_bits=0)
