@@ -102,8 +102,10 @@ int hmpc_modulus_root(hmpc_modulus* mod, uint64_t n, int inverse, uint32_t* root
  * bits (log2 elements a CTA stages; 0 = by shared-memory budget) and column
  * bits (coalescing width) -- or radix bits 0: the tensor-core engine (exact
  * fp16 MMAs over 8-bit digits, moduli of 2 to 8 limbs below
- * 0.996 * 2^(32L); tensor and CBD(V) producers; other calls of that shape
- * run the default tiles), whose local_bits selects the output split (1 or 2,
+ * 0.996 * 2^(32L); tensor, CBD(V) and forward uniform producers, the
+ * uniform draws written to the output by one launch before the groups run in
+ * place; other calls of that shape run the default tiles), whose local_bits
+ * selects the output split (1 or 2,
  * 0 = 1) of the group with contiguous rows; or radix bits 1: one thread-block
  * cluster of 8 CTAs per polynomial holding it in distributed shared memory,
  * one launch per transform (degrees 2^10..2^14, tensor producer; other calls
