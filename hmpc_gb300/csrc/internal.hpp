@@ -127,8 +127,18 @@ struct hmpc_context
         return true;
     }
 
+    // memory lent for the tensor-core digit buffers of the next calls instead
+    // of the context's own (a serving lane's share of its server's pool, so
+    // admission by memory counts it); nullptr: none
+    uint32_t* tc_lent = nullptr;
+    uint64_t tc_lent_words = 0;
+
     uint32_t* tc_scratch(uint64_t words)
     {
+        if (tc_lent && words <= tc_lent_words)
+        {
+            return tc_lent;
+        }
         if (words > tc_workspace_words)
         {
             if (tc_workspace)

@@ -164,7 +164,21 @@ struct hmpc_server
         return n * count * static_cast<uint64_t>(m->c.limbs);
     }
 
-    // scratch bytes of a dispatch of the given requests
+    // words of tensor-core digit buffers (two buffers of ceil((4L + 2) / 4)
+    // words per element) that a forward transform of `polys` polynomials
+    // takes when q's plan for that shape is the tensor-core engine, else 0
+    static uint64_t tc_words(hmpc_modulus* q, uint64_t n, uint64_t polys)
+    {
+        if (n < 16 || !tc_applicable(q, __builtin_ctzll(n), producer_tensor, nullptr) ||
+            !tc_plan_splits(q, n, polys))
+        {
+            return 0;
+        }
+        return 2 * ((4ull * static_cast<uint64_t>(q->c.limbs) + 5) / 4) * n * polys;
+    }
+
+    // scratch bytes of a dispatch of the given requests: buffers of its own
+    // and, after them, the digit buffers of a tensor-core transform
     uint64_t scratch_bytes(const std::vector<Request*>& rs) const
     {
         const hmpc_request& r0 = rs.front()->r;
@@ -177,20 +191,25 @@ struct hmpc_server
         switch (r0.kind)
         {
         case HMPC_REQUEST_NTT:
-            return single ? 0 : words_of(r0.q, r0.n, polys) * 4;
+            return ((single ? 0 : words_of(r0.q, r0.n, polys)) + tc_words(r0.q, r0.n, polys)) * 4;
         case HMPC_REQUEST_ENCRYPT:
         {
             const ResidentKey& k = keys[r0.key_id];
-            uint64_t w = 3 * words_of(k.q, k.n, polys);      // u, v/w, msg
-            if (!single)
-            {
-                w += words_of(k.p, k.n, polys) + 2 * words_of(k.q, k.n, polys);  // plaintext, c0, c1
-            }
-            return w * 4;
+            return (encrypt_words(k, polys, single) + tc_words(k.q, k.n, polys)) * 4;
         }
         default:
             return 0;
         }
+    }
+
+    static uint64_t encrypt_words(const ResidentKey& k, uint64_t polys, bool single)
+    {
+        uint64_t w = 3 * words_of(k.q, k.n, polys);  // u, v/w, msg
+        if (!single)
+        {
+            w += words_of(k.p, k.n, polys) + 2 * words_of(k.q, k.n, polys);  // plaintext, c0, c1
+        }
+        return w;
     }
 
     GroupKey group_of(const hmpc_request& r) const
@@ -218,6 +237,29 @@ struct hmpc_server
             polys += x->r.count;
         }
         uint32_t* scratch = reinterpret_cast<uint32_t*>(pool_base + d.offset);
+        // the lane's tensor-core digit buffers come from the dispatch's share
+        // of the pool, after its own buffers
+        struct Lend
+        {
+            hmpc_context* ctx;
+            ~Lend()
+            {
+                ctx->tc_lent = nullptr;
+                ctx->tc_lent_words = 0;
+            }
+        } lend{lane};
+        if (r0.kind == HMPC_REQUEST_NTT || r0.kind == HMPC_REQUEST_ENCRYPT)
+        {
+            const bool ntt = r0.kind == HMPC_REQUEST_NTT;
+            hmpc_modulus* q = ntt ? r0.q : keys[r0.key_id].q;
+            const uint64_t n = ntt ? r0.n : keys[r0.key_id].n;
+            const uint64_t own = ntt ? (single ? 0 : words_of(q, n, polys)) : encrypt_words(keys[r0.key_id], polys, single);
+            if (const uint64_t tw = tc_words(q, n, polys))
+            {
+                lane->tc_lent = scratch + own;
+                lane->tc_lent_words = tw;
+            }
+        }
         if (r0.kind == HMPC_REQUEST_NTT)
         {
             hmpc_modulus* q = r0.q;

@@ -149,3 +149,46 @@ def test_batching_window_groups_compatible_requests(queue):
         ct = lhe.enc(queue, key, m, q)
         assert (ct.c0.data == o[0].data).all().item() and (ct.c1.data == o[1].data).all().item()
     assert all(t is not None for t in tickets)
+
+
+def test_tensor_core_plans_inside_the_loop(queue, oracle):
+    """A modulus whose plan for a dispatch's shape is the tensor-core engine
+    runs that dispatch's transforms on it -- a transform request's and the
+    plaintext transform of an encryption -- with the digit buffers taken from
+    the server's pool; results equal the oracle and the library's encryption."""
+    import torch
+
+    p = queue.modulus(MODULI["p64"])
+    q = queue.modulus(MODULI["q256"])
+    om = oracle.Modulus(MODULI["q256"])
+    n, count = 1 << 12, 3
+    q.prepare(n)
+    p.prepare(n)
+    _, key = lhe.keygen(queue, q, p, n)
+    q.set_plan(n, count, False, radix_bits=0)
+    x = queue.uniform(q, (count,), n)
+    y = Tensor(q, (count,), n)
+    msgs = queue.uniform(p, (count,), n)
+    c0, c1 = Tensor(q, (count,), n), Tensor(q, (count,), n)
+    server = Server(queue, memory_budget=1 << 26, lanes=1, max_batch=1)
+    kid = server.add_key(q, p, key)
+    # warm the lane (tensor-core constants, error word), then count
+    server.submit_ntt(q, x, y)
+    server.drain()
+    queue.wait()
+    free_before = torch.cuda.mem_get_info()[0]
+    launches = server.stats()["launches"]
+    t = server.submit_ntt(q, x, y)
+    server.drain()
+    groups = (n.bit_length() - 1 + 2) // 3
+    assert server.stats()["launches"] - launches == groups
+    assert server.poll(t)[0] == 2
+    assert np.array_equal(y.numpy(), oracle.ntt(om, n, count, src=x.numpy()))
+    t = server.submit_encrypt(kid, q, msgs, c0, c1, [21, 0, 0])
+    server.drain()
+    assert server.poll(t)[0] == 2
+    assert torch.cuda.mem_get_info()[0] == free_before  # digit buffers from the pool
+    server.close()
+    queue.nonce = [21, 0, 0]
+    ct = lhe.enc(queue, key, msgs, q)
+    assert (ct.c0.data == c0.data).all().item() and (ct.c1.data == c1.data).all().item()
