@@ -22,6 +22,7 @@ import json
 import os
 import pathlib
 import statistics
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -264,6 +265,7 @@ def run_reference(args, world, rank):
                       "needs a SYCL compiler and C++23, absent here; the oracle restates its algorithm)",
             "keygen_amortised_over": sample,
             "gpu_arm_keygen_amortised_over": BATCH,
+            "sycl_toolchains": sycl_toolchains(),
         },
         "e2e": {"value": value, "unit": "encryptions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -674,6 +676,12 @@ def plain_encryption_comparison(queue, q, p, s, key, msgs, ct):
             "plain_decrypts_ok": ok}
 
 
+def sycl_toolchains():
+    """SYCL compilers on this host's PATH (the reference's own CPU build
+    needs one, with C++23); None where absent"""
+    return {name: shutil.which(name) for name in ("icpx", "dpcpp", "acpp", "syclcc", "clang++")}
+
+
 def cpu_baseline_sample(seconds=None):
     """The oracle's encryption timed on the host cores: batches of 16
     encryptions (fresh nonces each) until about `seconds` of CPU work (10 s by
@@ -709,6 +717,7 @@ def cpu_baseline_sample(seconds=None):
         "sample": f"{done} encryptions ({done // per} batches of {per}) at N=2^15, q 256-bit, CPU oracle "
                   f"(reference algorithm restated, OpenMP), {elapsed:.1f} s",
         "one_core": {"value": one / one_s, "cores": 1, "sample": f"{one} encryptions, {one_s:.2f} s"},
+        "sycl_toolchains": sycl_toolchains(),
     }
 
 
