@@ -121,7 +121,7 @@ def pin_to_gpu_cpus(device_index):
             os.sched_setaffinity(0, cpus)
             info["applied"] = True
     except Exception as e:  # no topology report: leave the process where it is
-        info["error"] = type(e).__name__
+        info["error"] = f"{type(e).__name__}: {e}"[:160]
     return info
 
 
