@@ -53,8 +53,17 @@ namespace hmpc_gb300
             {
                 return configured;
             }
-            tc_group_kernel<DC, R, IN, OUT, NS, Contig, Lay><<<grid, tc_workers<Contig> + 32, smem, stream>>>(p);
-            return cudaGetLastError();
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(grid);
+            cfg.blockDim = dim3(tc_workers<Contig> + 32);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = p.dependent ? 1u : 0u;
+            return cudaLaunchKernelEx(&cfg, tc_group_kernel<DC, R, IN, OUT, NS, Contig, Lay>, p);
         }
 
         template<int R, int IN, int NS>

@@ -108,6 +108,11 @@ namespace hmpc_gb300
         // batch is one buffer of `elements` words per plane)
         const uint32_t* const* in_polys;
         uint32_t* const* out_polys;
+        // launch with programmatic dependence on the kernel before it in the
+        // stream (another group of the same transform): this launch's CTAs set
+        // up while that one drains, and read its output only after it is
+        // complete (host side only)
+        uint32_t dependent;
     };
 
     // base-256 digits of the small-integer input (|x| < 2^70 for p < 2^64, 2V <= 64):
@@ -863,6 +868,9 @@ namespace hmpc_gb300
 
         const uint32_t tid = threadIdx.x;
         const uint32_t warp = tid >> 5, lane = tid & 31u;
+        // a dependent launch (the next group) may be scheduled once every CTA
+        // of this one is resident; its CTAs land on SMs as these exit
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
         const uint64_t t_begin = p.tiles * blockIdx.x / gridDim.x;
         const uint64_t t_end = p.tiles * (blockIdx.x + 1) / gridDim.x;
@@ -1072,6 +1080,12 @@ namespace hmpc_gb300
         else
         {
             // ------------------------------------------------ workers
+            // the kernel before this one in the stream (launched with
+            // programmatic dependence: the previous group) is complete and its
+            // writes visible before any digit is read or any output written;
+            // the constants the MMA thread streams meanwhile were complete
+            // before that kernel started
+            asm volatile("griddepcontrol.wait;" ::: "memory");
             constexpr bool in_blk = (Lay & 1) != 0;
             static_assert(!in_blk || (IN == tc_in_digits && Contig), "blocked input: adjacent rows");
             // word-major K where rows are columns of strided elements; the
