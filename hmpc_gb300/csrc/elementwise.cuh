@@ -182,9 +182,6 @@ namespace hmpc_gb300
                                                                    const uint32_t* stacked, uint64_t elements,
                                                                    const Modulus<L> m)
     {
-        // launched with programmatic dependence on the transform's last group:
-        // its blocks may be resident before that group completes
-        asm volatile("griddepcontrol.wait;" ::: "memory");
         const uint64_t stride = 3 * elements;
         const uint64_t mask = n - 1;
         for (uint64_t e = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < elements;

@@ -384,19 +384,9 @@ namespace hmpc_gb300
             {
                 return cudaSuccess;
             }
-            // programmatic dependence on the kernel before it (the stacked
-            // transform's last group): the kernel waits for it before any access
-            cudaLaunchConfig_t cfg{};
-            cfg.gridDim = dim3(grid_for(elements, 256));
-            cfg.blockDim = dim3(256);
-            cfg.stream = stream;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-            attr[0].val.programmaticStreamSerializationAllowed = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            return cudaLaunchKernelEx(&cfg, lhe_combine_pair_kernel<L>, c0, c1, ka, kb, n, stacked, elements,
-                                      device_modulus(h));
+            lhe_combine_pair_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(c0, c1, ka, kb, n, stacked,
+                                                                                   elements, device_modulus(h));
+            return cudaGetLastError();
         }
 
         cudaError_t matvec(uint32_t* z, const uint32_t* mat, const uint32_t* x, const MatvecParams& p,

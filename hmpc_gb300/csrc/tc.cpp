@@ -370,10 +370,10 @@ namespace hmpc_gb300::detail
         }
 
         // group j over `batch` polynomials; stride = plane stride of the digit / limb planes
-        // dependent: programmatic dependent launch (TcGroupParams::dependent;
-        // 0 for launches captured into graphs)
+        // dependent: the kernel before this one in the stream is another group
+        // of this call (programmatic dependent launch)
         int group(size_t j, const uint32_t* in, uint32_t* out, uint64_t stride, uint64_t batch, int in_kind,
-                  uint32_t vx2, const TcSmallInput* small, uint64_t msg_stride, uint32_t dependent = 0)
+                  uint32_t vx2, const TcSmallInput* small, uint64_t msg_stride, bool dependent = false)
         {
             const TcGroupPlan& gp = tt->groups[j];
             const bool first_sampled = j == 0 && (in_kind == tc_in_cbd || in_kind == tc_in_small);
@@ -387,7 +387,7 @@ namespace hmpc_gb300::detail
             p.rows = batch << gp.lo;
             p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
             p.tiles = gp.blocks * gp.shape.splits * p.tiles_per_block;
-            p.dependent = dependent;
+            p.dependent = dependent ? 1u : 0u;
             p.log_n = log_n;
             p.lo = gp.lo;
             p.spin_limit = ctx->tc_spin_limit;
@@ -482,7 +482,7 @@ namespace hmpc_gb300::detail
             const uint32_t* in = j == 0 ? src : digits + (((j - 1) & 1u) ? w * elements : 0);
             uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * elements : 0);
             if (int rc = run.group(j, in, o, elements, batch, j == 0 ? first_kind : tc_in_digits, vx2,
-                                   j == 0 ? small : nullptr, elements, j > 0 ? 1u : 2u))
+                                   j == 0 ? small : nullptr, elements, j > 0))
             {
                 return rc;
             }
@@ -541,7 +541,7 @@ namespace hmpc_gb300::detail
             uint32_t* slice = digits + static_cast<uint64_t>(i) * elements * (blocked ? w : 1);
             const int kind = parts[i].small ? tc_in_small : tc_in_cbd;
             if (int rc = run.group(0, nullptr, stages == 1 ? out + static_cast<uint64_t>(i) * elements : slice, total,
-                                   batch, kind, parts[i].vx2, parts[i].small, elements, i > 0 ? 1u : 2u))
+                                   batch, kind, parts[i].vx2, parts[i].small, elements, i > 0))
             {
                 return rc;
             }
@@ -553,7 +553,7 @@ namespace hmpc_gb300::detail
             const uint32_t* in = digits + (((j - 1) & 1u) ? w * total : 0);
             uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * total : 0);
             if (int rc = run.group(j, in, o, total, batch * static_cast<uint64_t>(count), tc_in_digits, 0, nullptr, 0,
-                                   1u))
+                                   true))
             {
                 return rc;
             }

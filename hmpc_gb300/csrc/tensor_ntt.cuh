@@ -109,12 +109,9 @@ namespace hmpc_gb300
         const uint32_t* const* in_polys;
         uint32_t* const* out_polys;
         // launch with programmatic dependence on the kernel before it in the
-        // stream: this launch's CTAs set up while that one drains, and the
-        // workers read digits or write outputs only after it is complete.
-        // 0: an ordinary launch; 1: the kernel before is another group of the
-        // same transform (the constants were complete before it started); 2:
-        // any kernel before (it may have built the constants: the MMA thread
-        // waits too before its first copy)
+        // stream (another group of the same transform): this launch's CTAs set
+        // up while that one drains, and read its output only after it is
+        // complete (host side only)
         uint32_t dependent;
     };
 
@@ -933,10 +930,6 @@ namespace hmpc_gb300
             // next block's constants stream in while the last tile finishes.
             if (lane == 0 && count)
             {
-                if (p.dependent == 2)
-                {
-                    asm volatile("griddepcontrol.wait;" ::: "memory");
-                }
                 constexpr uint32_t idesc = tc::f16_instr_descriptor(tc_rows, S::n_mma);
                 constexpr int ks_total = S::k_pad / 16;
                 constexpr int ks_half = NBUF == 1 ? (ks_total + 1) / 2 : ks_total;
