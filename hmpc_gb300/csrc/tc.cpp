@@ -387,6 +387,13 @@ namespace hmpc_gb300::detail
             p.rows = batch << gp.lo;
             p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
             p.tiles = gp.blocks * gp.shape.splits * p.tiles_per_block;
+            // launches captured into a graph keep ordinary dependences
+            cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+            if (dependent && cudaStreamIsCapturing(stream, &capture) == cudaSuccess &&
+                capture != cudaStreamCaptureStatusNone)
+            {
+                dependent = false;
+            }
             p.dependent = dependent ? 1u : 0u;
             p.log_n = log_n;
             p.lo = gp.lo;
