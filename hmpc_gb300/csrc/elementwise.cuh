@@ -202,63 +202,6 @@ namespace hmpc_gb300
         }
     }
 
-    template<int L>
-    __device__ __forceinline__ void load_pair(uint32_t (&x)[L], uint32_t (&y)[L], const uint32_t* t,
-                                              uint64_t elements, uint64_t e)
-    {
-#pragma unroll
-        for (int j = 0; j < L; ++j)
-        {
-            const uint2 v = *reinterpret_cast<const uint2*>(t + static_cast<uint64_t>(j) * elements + e);
-            x[j] = v.x;
-            y[j] = v.y;
-        }
-    }
-
-    template<int L>
-    __device__ __forceinline__ void store_pair(uint32_t* t, uint64_t elements, uint64_t e, const uint32_t (&x)[L],
-                                               const uint32_t (&y)[L])
-    {
-#pragma unroll
-        for (int j = 0; j < L; ++j)
-        {
-            *reinterpret_cast<uint2*>(t + static_cast<uint64_t>(j) * elements + e) = make_uint2(x[j], y[j]);
-        }
-    }
-
-    // lhe_combine_pair_kernel with two adjacent elements per thread (8-byte
-    // accesses, two independent product chains): elements and n even, every
-    // plane 8-byte aligned
-    template<int L>
-    __global__ void __launch_bounds__(256) lhe_combine_pair2_kernel(uint32_t* c0, uint32_t* c1, const uint32_t* ka,
-                                                                    const uint32_t* kb, uint64_t n,
-                                                                    const uint32_t* stacked, uint64_t elements,
-                                                                    const Modulus<L> m)
-    {
-        const uint64_t stride = 3 * elements;
-        const uint64_t mask = n - 1;
-        for (uint64_t e = 2 * (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x); e < elements;
-             e += 2 * static_cast<uint64_t>(gridDim.x) * blockDim.x)
-        {
-            uint32_t u0[L], u1[L], k0[L], k1[L], x0[L], x1[L];
-            load_pair<L>(u0, u1, stacked, stride, e);
-            load_pair<L>(k0, k1, ka, n, e & mask);
-            load_pair<L>(x0, x1, stacked + elements, stride, e);
-            mont_mul<L>(k0, k0, u0, m);
-            mont_mul<L>(k1, k1, u1, m);
-            mod_add<L>(x0, x0, k0, m);
-            mod_add<L>(x1, x1, k1, m);
-            store_pair<L>(c0, elements, e, x0, x1);
-            load_pair<L>(k0, k1, kb, n, e & mask);
-            load_pair<L>(x0, x1, stacked + 2 * elements, stride, e);
-            mont_mul<L>(k0, k0, u0, m);
-            mont_mul<L>(k1, k1, u1, m);
-            mod_add<L>(x0, x0, k0, m);
-            mod_add<L>(x1, x1, k1, m);
-            store_pair<L>(c1, elements, e, x0, x1);
-        }
-    }
-
     // ciphertext x ciphertext in NTT form: the tensor product
     // (d0, d1, d2) = (a0*b0, a0*b1 + a1*b0, a1*b1).  No counterpart in the
     // reference, whose ciphertexts only support linear operations

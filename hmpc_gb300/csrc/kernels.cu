@@ -384,18 +384,8 @@ namespace hmpc_gb300
             {
                 return cudaSuccess;
             }
-            const auto aligned = [](const void* ptr) { return (reinterpret_cast<uintptr_t>(ptr) & 7u) == 0; };
-            if (elements % 2 == 0 && n % 2 == 0 && aligned(c0) && aligned(c1) && aligned(ka) && aligned(kb) &&
-                aligned(stacked))
-            {
-                lhe_combine_pair2_kernel<L><<<grid_for(elements / 2, 256), 256, 0, stream>>>(
-                    c0, c1, ka, kb, n, stacked, elements, device_modulus(h));
-            }
-            else
-            {
-                lhe_combine_pair_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(c0, c1, ka, kb, n, stacked,
-                                                                                       elements, device_modulus(h));
-            }
+            lhe_combine_pair_kernel<L><<<grid_for(elements, 256), 256, 0, stream>>>(c0, c1, ka, kb, n, stacked,
+                                                                                   elements, device_modulus(h));
             return cudaGetLastError();
         }
 
