@@ -224,8 +224,8 @@ def run_reference(args, world, rank):
     q, p = oracle.Modulus(Q_256), oracle.Modulus(P_64)
     # keygen + 64 encryptions per step: keygen (two single-polynomial
     # transforms and a uniform draw, about half an encryption) is then under
-    # 1 % of a step, against its 1/256 share of the GPU step; the driver's
-    # 20 + 5 steps take about 35 s on 16 Arm cores
+    # 1 % of a step, against its 1/256 share of the GPU step; 20 timed and
+    # 5 warm-up steps take about 35 s on 16 Arm cores
     sample = max(1, int(os.environ.get("HMPC_REFERENCE_SAMPLE", "64")))
 
     def step():
