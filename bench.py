@@ -98,25 +98,30 @@ def pin_to_gpu_cpus(device_index):
                              capture_output=True, text=True, timeout=30).stdout
         smi_index = None
         for line in ids.splitlines():
-            idx, pci = [x.strip() for x in line.split(",")[:2]]
-            domain, bus, devfn = pci.split(":")  # e.g. 00000009:01:00.0
+            fields = [x.strip() for x in line.split(",")]
+            if len(fields) < 2 or not fields[0].isdigit() or fields[1].count(":") != 2:
+                continue
+            domain, bus, devfn = fields[1].split(":")  # e.g. 00000009:01:00.0
             if (int(domain, 16), int(bus, 16), int(devfn.split(".")[0], 16)) == want:
-                smi_index = int(idx)
+                smi_index = int(fields[0])
+        info["smi_index"] = smi_index
         topo = subprocess.run(["nvidia-smi", "topo", "-m"], capture_output=True, text=True, timeout=30).stdout
         lines = [l for l in topo.splitlines() if l.strip()]
-        header = next(l for l in lines if "CPU Affinity" in l)
+        # tab-separated columns; the header row has no label in its first cell
+        header = [c.strip() for c in next(l for l in lines if "CPU Affinity" in l).split("\t")]
+        row = [c.strip() for c in next(l for l in lines if smi_index is not None and
+                                       l.startswith(f"GPU{smi_index}\t")).split("\t")]
         col = header.index("CPU Affinity")
-        row = next(l for l in lines if smi_index is not None and l.split()[0] == f"GPU{smi_index}")
-        field = row[col:].split()[0]
+        field = row[col] if col < len(row) else ""
+        info["gpu_cpus"] = field
         cpus = set()
         for part in field.split(","):
-            if "-" in part:
-                a, b = part.split("-")
-                cpus.update(range(int(a), int(b) + 1))
+            ends = part.split("-")
+            if len(ends) == 2 and ends[0].isdigit() and ends[1].isdigit():
+                cpus.update(range(int(ends[0]), int(ends[1]) + 1))
             elif part.isdigit():
                 cpus.add(int(part))
         cpus &= set(os.sched_getaffinity(0))
-        info["gpu_cpus"] = field
         if cpus:
             os.sched_setaffinity(0, cpus)
             info["applied"] = True
@@ -985,31 +990,50 @@ def main():
         b["done"].record(stream)
     os.sched_setaffinity(0, cpu_set)
 
-    def e2e_step(i):
+    # Host enqueue order per step i: the encryption of step i, then the
+    # copy-out of step i - 1, then the copy-in of step i + 1.  Each copy waits
+    # for an encryption that was enqueued before the next one, so the copies
+    # overlap the following encryption even where the device takes all
+    # streams' work through one queue in enqueue order.
+    def load(i):
         b = sets[i % 2]
         copy_in.wait_event(b["done"])  # the set's plaintexts are no longer read
         with torch.cuda.stream(copy_in):
             b["msgs"].data.copy_(host_msgs, non_blocking=True)
         b["loaded"].record(copy_in)
+
+    def encrypt(i):
+        b = sets[i % 2]
         stream.wait_event(b["loaded"])
         stream.wait_event(b["read"])  # the set's previous ciphertexts are copied out
         _lib.call("hmpc_lhe_keygen", queue.handle, q.handle, p.handle, N, s.ptr(), key.a.ptr(), key.b.ptr())
         lhe.enc(queue, key, b["msgs"], q, out=b["ct"])
         b["done"].record(stream)
+
+    def read(i):
+        b = sets[i % 2]
         copy_out.wait_event(b["done"])
         with torch.cuda.stream(copy_out):
             b["c0"].copy_(b["ct"].c0.data, non_blocking=True)
             b["c1"].copy_(b["ct"].c1.data, non_blocking=True)
         b["read"].record(copy_out)
 
-    for i in range(args.warmup):
-        e2e_step(i)
+    def e2e_run(count):
+        load(0)
+        for i in range(count):
+            encrypt(i)
+            if i > 0:
+                read(i - 1)
+            if i + 1 < count:
+                load(i + 1)
+        read(count - 1)
+
+    e2e_run(args.warmup)
     barrier()
     e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e_start.record(stream)
     copy_in.wait_stream(stream)
-    for i in range(args.steps):
-        e2e_step(i)
+    e2e_run(args.steps)
     stream.wait_stream(copy_out)
     e_stop.record(stream)
     barrier()
@@ -1037,19 +1061,27 @@ def main():
         link[name] = 3 * src.numel() * 4 / (c_start.elapsed_time(c_stop) * 1e-3) / 1e9
     copy_s = max(host_msgs.numel() * 4 / (link["h2d"] * 1e9),
                  (host_c0.numel() + host_c1.numel()) * 4 / (link["d2h"] * 1e9))
-    # the same device-to-host copy while a step computes on the queue's
-    # stream: equal to the rate alone when copies and kernels overlap
-    c_start, c_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # whether copies and kernels overlap here: one step with a device-to-host
+    # copy of the same length as the step's on the copy-out stream beside it,
+    # timed as a whole on the queue's stream, against the step alone
     barrier()
+    o_start, o_mid, o_stop = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    o_start.record(stream)
     step(msgs)
+    o_mid.record(stream)
+    copy_out.wait_event(o_mid)
     with torch.cuda.stream(copy_out):
-        c_start.record(copy_out)
-        for _ in range(3):
-            host_c0.copy_(sets[0]["ct"].c0.data, non_blocking=True)
-        c_stop.record(copy_out)
+        host_c0.copy_(sets[0]["ct"].c0.data, non_blocking=True)
+        host_c1.copy_(sets[0]["ct"].c1.data, non_blocking=True)
     step(msgs)
+    stream.wait_stream(copy_out)
+    o_stop.record(stream)
     barrier()
-    link["d2h_during_compute"] = 3 * host_c0.numel() * 4 / (c_start.elapsed_time(c_stop) * 1e-3) / 1e9
+    alone_ms = o_start.elapsed_time(o_mid)
+    both_ms = o_mid.elapsed_time(o_stop)
+    link["step_ms"] = alone_ms
+    link["step_with_copy_out_ms"] = both_ms  # about step_ms where they overlap, + copy time where not
+    link["device_max_connections"] = os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")
 
     # ------------------------------------------- dominant kernel roofline
     # the fused CBD(10) -> NTT over the batch: the transform's kernel launches
