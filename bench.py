@@ -1077,25 +1077,6 @@ def main():
         link[name] = 3 * src.numel() * 4 / (c_start.elapsed_time(c_stop) * 1e-3) / 1e9
     copy_s = max(host_msgs.numel() * 4 / (link["h2d"] * 1e9),
                  (host_c0.numel() + host_c1.numel()) * 4 / (link["d2h"] * 1e9))
-    # the step's device-to-host copy beside the next step: its own duration
-    # on the copy-out stream and the step's on the queue's stream (about the
-    # copy alone and the step alone where copies and kernels overlap)
-    barrier()
-    o_mid, o_stop, c_start, c_stop = (torch.cuda.Event(enable_timing=True) for _ in range(4))
-    step(msgs)
-    o_mid.record(stream)
-    copy_out.wait_event(o_mid)
-    with torch.cuda.stream(copy_out):
-        c_start.record(copy_out)
-        host_c0.copy_(sets[0]["ct"].c0.data, non_blocking=True)
-        host_c1.copy_(sets[0]["ct"].c1.data, non_blocking=True)
-        c_stop.record(copy_out)
-    step(msgs)
-    o_stop.record(stream)
-    barrier()
-    link["copy_out_beside_step_ms"] = c_start.elapsed_time(c_stop)
-    link["step_beside_copy_out_ms"] = o_mid.elapsed_time(o_stop)
-    link["device_max_connections"] = os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")
 
     # ------------------------------------------- dominant kernel roofline
     # the fused CBD(10) -> NTT over the batch: the transform's kernel launches
