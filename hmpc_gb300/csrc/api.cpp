@@ -208,9 +208,15 @@ namespace hmpc_gb300::detail
         options.col_bits = choice.col_bits;
         const std::vector<PassPlan> plan = plan_transform(L, log_n, batch, inverse, choice.radix_bits, options);
         const RngKey rng = ctx->rng();
+        // passes after the first launch with programmatic dependence on the
+        // pass before (ordinary launches while the stream is being captured)
+        cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+        const bool capturing =
+            cudaStreamIsCapturing(ctx->stream, &capture) == cudaSuccess && capture != cudaStreamCaptureStatusNone;
         for (size_t i = 0; i < plan.size(); ++i)
         {
             NttPassParams p = plan[i].params;
+            p.dependent = i > 0 && !capturing ? 1u : 0u;
             p.out = out;
             p.src = i == 0 ? src : nullptr;
             p.twiddles = inverse ? t->inverse : t->forward;

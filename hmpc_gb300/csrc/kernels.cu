@@ -66,8 +66,17 @@ namespace hmpc_gb300
                 }
                 configured = true;
             }
-            kernel<<<grid, block, smem, stream>>>(p, m);
-            return cudaGetLastError();
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(grid);
+            cfg.blockDim = dim3(block);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = p.dependent ? 1u : 0u;
+            return cudaLaunchKernelEx(&cfg, kernel, p, m);
         }
 
         template<int RB>

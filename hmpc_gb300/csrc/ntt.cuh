@@ -71,6 +71,9 @@ namespace hmpc_gb300
         // what the request would draw alone with its own nonce.
         const uint32_t* poly_rng;
         uint32_t rng_slot;
+        // host side: launch with programmatic dependence on the pass before
+        // it in the stream (a pass of the same transform)
+        uint32_t dependent;
     };
 
     __device__ __forceinline__ uint32_t smem_addr(uint32_t local)
@@ -416,6 +419,11 @@ namespace hmpc_gb300
     __global__ void __launch_bounds__(256, (R >= 3 ? 2 : 3)) ntt_pass_kernel(const NttPassParams p,
                                                                             const Modulus<L> m)
     {
+        // the next pass may be scheduled once every CTA of this one has
+        // started; a pass launched with programmatic dependence on the one
+        // before proceeds once that one is complete and its writes visible
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+        asm volatile("griddepcontrol.wait;" ::: "memory");
         extern __shared__ uint32_t smem[];
         ntt_process<L, R, Kind, NW>(p, m, static_cast<uint64_t>(blockIdx.x) << p.tile_bits, smem);
     }
