@@ -34,18 +34,54 @@ namespace hmpc_gb300
         b = __funnelshift_l(b ^ c, b ^ c, 7);
     }
 
-    __device__ __forceinline__ void chacha20_block(const RngKey& k, uint32_t counter, uint32_t (&out)[16])
+    // The part of a block's first round that every block of one key and
+    // nonce shares: the column quarter rounds of columns 1-3 (constants, key
+    // words, nonce; the counter is in column 0) and the first addition of
+    // column 0.  Computed once, it saves three of the block's eighty quarter
+    // rounds for each further block.
+    struct ChachaPre
     {
-        uint32_t x[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u, k.key[0], k.key[1], k.key[2],
-                          k.key[3], k.key[4], k.key[5], k.key[6], k.key[7], counter, k.nonce[0], k.nonce[1],
-                          k.nonce[2]};
+        uint32_t x[16];  // the state after those steps (x[12], the counter, unset)
+    };
+
+    __device__ __forceinline__ ChachaPre chacha_pre(const RngKey& k)
+    {
+        ChachaPre p{{0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u, k.key[0], k.key[1], k.key[2], k.key[3],
+                     k.key[4], k.key[5], k.key[6], k.key[7], 0u, k.nonce[0], k.nonce[1], k.nonce[2]}};
+        chacha_quarter(p.x[1], p.x[5], p.x[9], p.x[13]);
+        chacha_quarter(p.x[2], p.x[6], p.x[10], p.x[14]);
+        chacha_quarter(p.x[3], p.x[7], p.x[11], p.x[15]);
+        p.x[0] += p.x[4];
+        return p;
+    }
+
+    __device__ __forceinline__ void chacha20_block(const ChachaPre& pre, const RngKey& k, uint32_t counter,
+                                                   uint32_t (&out)[16])
+    {
+        uint32_t x[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+        {
+            x[i] = pre.x[i];
+        }
+        // the rest of column 0's first quarter round (a += b is in pre)
+        x[12] = __funnelshift_l(counter ^ x[0], counter ^ x[0], 16);
+        x[8] += x[12];
+        x[4] = __funnelshift_l(x[4] ^ x[8], x[4] ^ x[8], 12);
+        x[0] += x[4];
+        x[12] = __funnelshift_l(x[12] ^ x[0], x[12] ^ x[0], 8);
+        x[8] += x[12];
+        x[4] = __funnelshift_l(x[4] ^ x[8], x[4] ^ x[8], 7);
 #pragma unroll
         for (int r = 0; r < 10; ++r)
         {
-            chacha_quarter(x[0], x[4], x[8], x[12]);
-            chacha_quarter(x[1], x[5], x[9], x[13]);
-            chacha_quarter(x[2], x[6], x[10], x[14]);
-            chacha_quarter(x[3], x[7], x[11], x[15]);
+            if (r > 0)
+            {
+                chacha_quarter(x[0], x[4], x[8], x[12]);
+                chacha_quarter(x[1], x[5], x[9], x[13]);
+                chacha_quarter(x[2], x[6], x[10], x[14]);
+                chacha_quarter(x[3], x[7], x[11], x[15]);
+            }
             chacha_quarter(x[0], x[5], x[10], x[15]);
             chacha_quarter(x[1], x[6], x[11], x[12]);
             chacha_quarter(x[2], x[7], x[8], x[13]);
@@ -66,17 +102,23 @@ namespace hmpc_gb300
         out[15] = x[15] + k.nonce[2];
     }
 
+    __device__ __forceinline__ void chacha20_block(const RngKey& k, uint32_t counter, uint32_t (&out)[16])
+    {
+        chacha20_block(chacha_pre(k), k, counter, out);
+    }
+
     // The first `Words` words of the stream that starts at block `counter`
     // (blocks counter, counter+1, ... as the generator refills).
     template<int Words>
-    __device__ __forceinline__ void chacha_stream(const RngKey& k, uint32_t counter, uint32_t (&w)[Words])
+    __device__ __forceinline__ void chacha_stream(const ChachaPre& pre, const RngKey& k, uint32_t counter,
+                                                  uint32_t (&w)[Words])
     {
         constexpr int blocks = (Words + 15) / 16;
 #pragma unroll
         for (int b = 0; b < blocks; ++b)
         {
             uint32_t blk[16];
-            chacha20_block(k, counter + static_cast<uint32_t>(b), blk);
+            chacha20_block(pre, k, counter + static_cast<uint32_t>(b), blk);
 #pragma unroll
             for (int i = 0; i < 16; ++i)
             {
@@ -86,6 +128,12 @@ namespace hmpc_gb300
                 }
             }
         }
+    }
+
+    template<int Words>
+    __device__ __forceinline__ void chacha_stream(const RngKey& k, uint32_t counter, uint32_t (&w)[Words])
+    {
+        chacha_stream<Words>(chacha_pre(k), k, counter, w);
     }
 
     // Centred binomial value popcount(low 4V bits) - 2V from words

@@ -387,12 +387,13 @@ namespace hmpc_gb300
     // variances (2V = 1 for the secret and u, 2V = 20 for the noise) take
     // compile-time word counts, so only the keystream words they consume are
     // computed and the masks fold away; other variances draw eight words.
-    __device__ __forceinline__ void tc_cbd_pair(const TcGroupParams& p, uint32_t counter, int& a, int& b)
+    __device__ __forceinline__ void tc_cbd_pair(const TcGroupParams& p, const ChachaPre& pre, uint32_t counter,
+                                                int& a, int& b)
     {
         if (p.vx2 == 20)
         {
             uint32_t w[4];
-            chacha_stream<4>(p.rng, counter, w);
+            chacha_stream<4>(pre, p.rng, counter, w);
             a = __popc(w[0]) + __popc(w[1] & 0xffu) - 20;
             b = __popc(w[2]) + __popc(w[3] & 0xffu) - 20;
             return;
@@ -400,7 +401,7 @@ namespace hmpc_gb300
         if (p.vx2 == 1)
         {
             uint32_t w[2];
-            chacha_stream<2>(p.rng, counter, w);
+            chacha_stream<2>(pre, p.rng, counter, w);
             a = __popc(w[0] & 3u) - 1;
             b = __popc(w[1] & 3u) - 1;
             return;
@@ -408,7 +409,7 @@ namespace hmpc_gb300
         const int count = 2 * static_cast<int>(p.vx2);
         const int nw = static_cast<int>(p.nw);
         uint32_t w[8];
-        chacha_stream<8>(p.rng, counter, w);
+        chacha_stream<8>(pre, p.rng, counter, w);
         a = 0;
         b = 0;
 #pragma unroll
@@ -436,7 +437,8 @@ namespace hmpc_gb300
     // index of the first element, first draw for m, second for m + 4
     // (number_theoretic_transform.hpp:316-329, comp/queue.hpp:191-212); thread
     // (row, part) draws the pair m = part
-    __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t tid)
+    __device__ __forceinline__ void tc_store_cbd(const TcGroupParams& p, const ChachaPre& pre, uint8_t* sa,
+                                                 uint32_t mt, uint32_t tid)
     {
         // the four threads of a row are adjacent lanes: a warp's stores cover eight whole segment rows
         const uint32_t row = tid >> 2, part = tid & 3u;
@@ -445,7 +447,7 @@ namespace hmpc_gb300
         if (r.ok)
         {
             const uint64_t idx = r.base + (static_cast<uint64_t>(part) << p.lo);
-            tc_cbd_pair(p, static_cast<uint32_t>(idx), e_u, e_v);
+            tc_cbd_pair(p, pre, static_cast<uint32_t>(idx), e_u, e_v);
         }
         uint8_t* seg = sa + tc::operand_offset(row, 0, tc_rows);
         const __half hu = __int2half_rn(e_u), hv = __int2half_rn(e_v);
@@ -491,7 +493,8 @@ namespace hmpc_gb300
     // the pair m = part, m + 4), m the plaintext residue of the same element;
     // x (|x| < 2^70) is written as its 8 low bytes (unsigned digits) and the
     // signed value x >> 64 (K index = a * 8 + m)
-    __device__ __forceinline__ void tc_store_small(const TcGroupParams& p, uint8_t* sa, uint32_t mt, uint32_t tid)
+    __device__ __forceinline__ void tc_store_small(const TcGroupParams& p, const ChachaPre& pre, uint8_t* sa,
+                                                   uint32_t mt, uint32_t tid)
     {
         const uint32_t row = tid >> 2, part = tid & 3u;
         const TcRow r = tc_row<3>(p, 0, mt, row);
@@ -513,7 +516,7 @@ namespace hmpc_gb300
                 }
             }
             int a = 0, b = 0;
-            tc_cbd_pair(p, static_cast<uint32_t>(idx), a, b);
+            tc_cbd_pair(p, pre, static_cast<uint32_t>(idx), a, b);
             const uint64_t pval = p.pq[0] | (p.msg_limbs > 1 ? static_cast<uint64_t>(p.pq[1]) << 32 : 0ull);
             x[0] = static_cast<__int128>(pval) * a;
             x[1] = static_cast<__int128>(pval) * b;
@@ -1099,6 +1102,8 @@ namespace hmpc_gb300
                     loader.load(p, cur.hb / NS, cur.mt, tid);
                 }
             }
+            // the sampling loaders' keystream blocks share one key and nonce
+            const ChachaPre pre = S::generated ? chacha_pre(p.rng) : ChachaPre{};
             TcCursor prev = cur;
             for (uint64_t i = 0; i <= count; ++i)
             {
@@ -1121,11 +1126,11 @@ namespace hmpc_gb300
                     }
                     if constexpr (IN == tc_in_cbd)
                     {
-                        tc_store_cbd(p, sa, cur.mt, tid);
+                        tc_store_cbd(p, pre, sa, cur.mt, tid);
                     }
                     else if constexpr (IN == tc_in_small)
                     {
-                        tc_store_small(p, sa, cur.mt, tid);
+                        tc_store_small(p, pre, sa, cur.mt, tid);
                     }
                     else
                     {
