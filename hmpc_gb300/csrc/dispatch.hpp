@@ -120,6 +120,9 @@ namespace hmpc_gb300
         bool (*shape)(int r, int in_kind, int out_kind, int splits, TcShapeInfo& out);
         cudaError_t (*gen)(const TcGenParams& p, const HostModulus& m, cudaStream_t stream);
         cudaError_t (*expand)(const TcExpandParams& p, const HostModulus& m, cudaStream_t stream);
+        // the first six forward stages of CBD-fed transforms as one group (tc_wide_kernel)
+        cudaError_t (*combine6)(const TcCombineParams& p, const HostModulus& m, cudaStream_t stream);
+        cudaError_t (*wide)(const TcGroupParams& p, unsigned grid, cudaStream_t stream);
     };
 
     const TcKernels* tc_kernels_2();

@@ -56,6 +56,12 @@ namespace hmpc_gb300::detail
         bool fit = true;
         // the largest sum of |digit| over one column of the digit-fed groups' images
         uint32_t column_max = 0;
+        // the first six forward stages as one group fed by CBD samples
+        // (tc_wide_kernel): constants G6 * R, and G6 * p * R for the p-scaled
+        // draws of the encryption (p: the plaintext modulus they were built for)
+        uint8_t* wide_cbd = nullptr;
+        uint8_t* wide_cbd_p = nullptr;
+        std::vector<uint32_t> wide_p;
     };
 
     // The carry of a group fed by digits takes two operations per digit while

@@ -301,6 +301,142 @@ namespace
         *out = &mod->tc_tables[key];
         return HMPC_OK;
     }
+
+    // whether a forward plan starts with two three-stage groups and has at
+    // least two more after them (the wide group replaces the first two)
+    bool wide_plan(const TcTables* tt)
+    {
+        // the second group must write plain planes (not the blocked runs of a
+        // group before the last)
+        return tt->groups.size() >= 4 && tt->groups[0].g == 3 && tt->groups[1].g == 3 &&
+               (tt->groups[1].layout & 2) == 0;
+    }
+
+    // the wide group's images: unscaled, and scaled by p (nullptr: not needed)
+    int prepare_wide(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, TcTables* tt, const hmpc_modulus* p)
+    {
+        const int L = mod->c.limbs;
+        std::vector<uint32_t> pwords;
+        if (p)
+        {
+            pwords.assign(p->c.q.begin(), p->c.q.end());
+        }
+        Tables* t = nullptr;
+        if (int rc = mod->prepare(n, &t))
+        {
+            return rc;
+        }
+        std::lock_guard<std::mutex> lock(mod->tables_mutex);
+        const bool need_plain = !tt->wide_cbd;
+        const bool need_p = p && (!tt->wide_cbd_p || tt->wide_p != pwords);
+        if (!need_plain && !need_p)
+        {
+            return HMPC_OK;
+        }
+        const TcKernels* k = kernels_of(mod);
+        const int log_n = __builtin_ctzll(n);
+        const uint32_t image_bytes = tc_wide_b_bytes;
+        const size_t images_bytes = static_cast<size_t>(tc_wide_splits) * image_bytes;
+        uint32_t *gx_a = nullptr, *gx_b = nullptr, *gx6 = nullptr, *d_pow = nullptr, *d_scale = nullptr;
+        auto cleanup = [&]() {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(gx_a);
+            cudaFree(gx_b);
+            cudaFree(gx6);
+            cudaFree(d_pow);
+            cudaFree(d_scale);
+        };
+        if (cudaMalloc(&gx_a, 64u * L * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&gx_b, 8u * 64u * L * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&gx6, 64u * 64u * L * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&d_pow, L * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&d_scale, L * sizeof(uint32_t)) != cudaSuccess)
+        {
+            cleanup();
+            return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core generation scratch");
+        }
+        // the first two groups' matrices in Montgomery form
+        for (int j = 0; j < 2; ++j)
+        {
+            const TcGroupPlan& gp = tt->groups[static_cast<size_t>(j)];
+            TcGenParams gen{};
+            gen.twiddles = t->forward;
+            gen.gx = j == 0 ? gx_a : gx_b;
+            gen.blocks = gp.blocks;
+            gen.log_n = static_cast<uint32_t>(log_n);
+            gen.inverse = 0;
+            gen.s0 = gp.s0;
+            gen.g = gp.g;
+            gen.lo = gp.lo;
+            gen.montgomery = 1;
+            if (cudaError_t e = k->gen(gen, mod->h, ctx->stream))
+            {
+                cleanup();
+                return cuda_fail(e, "generating tensor-core constants");
+            }
+        }
+        // raw samples: one digit slot, 256^0 * R
+        const host::words one = host::to_mont(mod->c, host::words{1u});
+        cudaMemcpyAsync(d_pow, one.data(), L * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+        for (int variant = 0; variant < 2; ++variant)
+        {
+            if ((variant == 0 && !need_plain) || (variant == 1 && !need_p))
+            {
+                continue;
+            }
+            TcCombineParams cp{};
+            cp.gx_a = gx_a;
+            cp.gx_b = gx_b;
+            cp.gx = gx6;
+            if (variant == 1)
+            {
+                const host::words pm = host::to_mont(mod->c, p->c.q);
+                cudaMemcpyAsync(d_scale, pm.data(), L * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+                cp.scale = d_scale;
+            }
+            if (cudaError_t e = k->combine6(cp, mod->h, ctx->stream))
+            {
+                cleanup();
+                return cuda_fail(e, "combining tensor-core constants");
+            }
+            uint8_t*& images = variant == 0 ? tt->wide_cbd : tt->wide_cbd_p;
+            if (!images && cudaMalloc(&images, images_bytes) != cudaSuccess)
+            {
+                cleanup();
+                return fail(HMPC_ERROR_OUT_OF_MEMORY, "allocating tensor-core constants");
+            }
+            cudaMemsetAsync(images, 0, images_bytes, ctx->stream);
+            TcExpandParams ex{};
+            ex.gx = gx6;
+            ex.pow256 = d_pow;
+            ex.images = images;
+            ex.blocks = 1;
+            ex.r = tc_wide_r;
+            ex.dc = static_cast<uint32_t>(k->digits);
+            ex.d_in = 1;
+            ex.splits = tc_wide_splits;
+            ex.n_mma = 256;
+            ex.image_bytes = image_bytes;
+            ex.word_major = 0;
+            for (int j = 0; j < L; ++j)
+            {
+                ex.half[j] = mod->c.half[static_cast<size_t>(j)];
+            }
+            if (cudaError_t e = k->expand(ex, mod->h, ctx->stream))
+            {
+                cleanup();
+                return cuda_fail(e, "expanding tensor-core constants");
+            }
+            // gx6 is reused by the next variant
+            cudaStreamSynchronize(ctx->stream);
+        }
+        cleanup();
+        if (need_p)
+        {
+            tt->wide_p = pwords;
+        }
+        return HMPC_OK;
+    }
 }
 
 namespace hmpc_gb300::detail
@@ -443,6 +579,36 @@ namespace hmpc_gb300::detail
             ++ctx->launches;
             return HMPC_OK;
         }
+
+        // the first six stages of `batch` CBD(vx2)-fed transforms in one wide
+        // group (images: the eight images of G6 or G6 * p), written as digit
+        // planes of plane stride `stride` at `out`
+        int wide(const uint8_t* images, uint32_t* out, uint64_t stride, uint64_t batch, uint32_t vx2)
+        {
+            TcGroupParams p{};
+            p.out = out;
+            p.images = images;
+            p.error = ctx->tc_error;
+            p.elements = stride;
+            p.lo = log_n - 6;
+            p.rows = batch << p.lo;
+            p.tiles_per_block = static_cast<uint32_t>((p.rows + tc_rows - 1) / tc_rows);
+            p.tiles = p.tiles_per_block;
+            p.log_n = log_n;
+            p.spin_limit = ctx->tc_spin_limit;
+            p.rng = ctx->rng();
+            p.vx2 = vx2;
+            p.nw = (2 * vx2 + 31) / 32;
+            const unsigned grid =
+                static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
+            cudaError_t e = k->wide(p, grid, stream);
+            if (e != cudaSuccess)
+            {
+                return cuda_fail(e, "launching the wide tensor-core group");
+            }
+            ++ctx->launches;
+            return HMPC_OK;
+        }
     };
 
     int run_tc_transform(hmpc_context* ctx, hmpc_modulus* mod, uint64_t n, uint64_t batch, bool inverse, int kind,
@@ -539,6 +705,69 @@ namespace hmpc_gb300::detail
         if (int rc = run.init(ctx, mod, n, tt))
         {
             return rc;
+        }
+        // Parts fed by CBD samples alone (or p times them) take the first six
+        // stages in one wide group into their slice of buffer 1; the others
+        // their first group into buffer 0 and the second from there into
+        // buffer 1 -- the shared groups then start at the third.  Launch order
+        // (and so nonce order) stays the parts' order.
+        const hmpc_modulus* scale_p = nullptr;
+        bool any_wide = false;
+        for (int i = 0; i < count; ++i)
+        {
+            if (!parts[i].small)
+            {
+                any_wide = true;
+            }
+            else if (!parts[i].small->msg)
+            {
+                any_wide = true;
+                scale_p = parts[i].small->p;
+            }
+        }
+        const bool use_wide = any_wide && wide_plan(tt);
+        if (use_wide)
+        {
+            if (int rc = prepare_wide(ctx, mod, n, tt, scale_p))
+            {
+                return rc;
+            }
+            for (int i = 0; i < count; ++i)
+            {
+                uint32_t* slice0 = digits + static_cast<uint64_t>(i) * elements;
+                uint32_t* slice1 = digits + w * total + static_cast<uint64_t>(i) * elements;
+                if (!parts[i].small || !parts[i].small->msg)
+                {
+                    const uint8_t* images = parts[i].small ? tt->wide_cbd_p : tt->wide_cbd;
+                    if (int rc = run.wide(images, slice1, total, batch, parts[i].vx2))
+                    {
+                        return rc;
+                    }
+                    nonce_add(ctx->nonce, elements);
+                    continue;
+                }
+                if (int rc = run.group(0, nullptr, slice0, total, batch, tc_in_small, parts[i].vx2, parts[i].small,
+                                       elements, i > 0))
+                {
+                    return rc;
+                }
+                nonce_add(ctx->nonce, elements);
+                if (int rc = run.group(1, slice0, slice1, total, batch, tc_in_digits, 0, nullptr, 0, true))
+                {
+                    return rc;
+                }
+            }
+            for (size_t j = 2; j < stages; ++j)
+            {
+                const uint32_t* in = digits + (((j - 1) & 1u) ? w * total : 0);
+                uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * total : 0);
+                if (int rc = run.group(j, in, o, total, batch * static_cast<uint64_t>(count), tc_in_digits, 0, nullptr,
+                                       0, true))
+                {
+                    return rc;
+                }
+            }
+            return HMPC_OK;
         }
         // first groups: part i into its slice of buffer 0 (plane-major slices,
         // or whole blocked runs when the next group is the last)

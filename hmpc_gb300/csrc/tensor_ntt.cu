@@ -206,7 +206,29 @@ namespace hmpc_gb300
             return cudaGetLastError();
         }
 
-        const TcKernels table = {DC, group, shape, gen, expand};
+        cudaError_t combine6(const TcCombineParams& p, const HostModulus& h, cudaStream_t stream)
+        {
+            tc_combine6_kernel<L><<<16, 256, 0, stream>>>(p, device_modulus(h));
+            return cudaGetLastError();
+        }
+
+        cudaError_t wide(const TcGroupParams& p, unsigned grid, cudaStream_t stream)
+        {
+            static std::once_flag once;
+            static cudaError_t configured = cudaSuccess;
+            std::call_once(once, [] {
+                configured = cudaFuncSetAttribute(tc_wide_kernel<DC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  tc_wide_smem);
+            });
+            if (configured != cudaSuccess)
+            {
+                return configured;
+            }
+            tc_wide_kernel<DC><<<grid, 512 + 32, tc_wide_smem, stream>>>(p);
+            return cudaGetLastError();
+        }
+
+        const TcKernels table = {DC, group, shape, gen, expand, combine6, wide};
     }
 
     const TcKernels* HMPC_CAT(tc_kernels_, HMPC_L)()

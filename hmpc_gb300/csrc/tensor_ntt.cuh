@@ -713,7 +713,7 @@ namespace hmpc_gb300
     __device__ __forceinline__ void tc_epilogue(const TcGroupParams& p, uint32_t tmem, const TcCursor& cur,
                                                 uint32_t warp, uint32_t lane)
     {
-        constexpr int g = R == 8 ? 3 : (R == 4 ? 2 : 1);
+        constexpr int g = R == 64 ? 6 : (R == 8 ? 3 : (R == 4 ? 2 : 1));
         constexpr int L = DC / 4;
         constexpr int W = (DC + 2 + 3) / 4;
         constexpr int outputs = R / NS;
@@ -1191,6 +1191,269 @@ namespace hmpc_gb300
         }
     }
 
+    // ------------------------------------------------------------- wide group
+    // The first six forward stages of a transform fed by centred binomial
+    // samples, in one group of r = 64: the samples are single digits, so the
+    // 64 x 64 constant of the one block (the product of the first two
+    // three-stage groups' matrices) streams through shared memory in eight
+    // images of eight outputs each (K = 64, N = 256), while each 128-row
+    // digit tile -- 8192 elements, one generator per stage-0 pair (m, m + 32)
+    // -- is drawn once.  Per row tile: the workers draw and store the tile,
+    // then carry out the eight accumulators as the MMA thread fills them
+    // (two TMEM buffers of 256 columns, two image buffers).
+    constexpr int tc_wide_r = 64;
+    constexpr int tc_wide_splits = 8;
+    constexpr uint32_t tc_wide_a_bytes = tc_rows * tc_wide_r * 2;       // K = 64 fp16
+    constexpr uint32_t tc_wide_b_bytes = tc_wide_r * 256 * 2;           // K = 64, N = 256
+    constexpr uint32_t tc_wide_control = 128;
+    // at least half of an SM's shared memory: one CTA per SM, so its two
+    // accumulators (all 512 TMEM columns) are always free
+    constexpr uint32_t tc_wide_smem = 116u * 1024u;
+    static_assert(tc_wide_a_bytes + 2 * tc_wide_b_bytes + tc_wide_control <= tc_wide_smem, "wide group smem");
+
+    // the tile's CBD samples: thread (row, part) draws the pairs m = part + 4j
+    // (j < 8) of its row: generator counter = index of element m, first
+    // draw for m, second for m + 32 (number_theoretic_transform.hpp:316-329)
+    __device__ __forceinline__ void tc_store_cbd_wide(const TcGroupParams& p, const ChachaPre& pre, uint8_t* sa,
+                                                      uint32_t mt, uint32_t tid)
+    {
+        const uint32_t row = tid >> 2, part = tid & 3u;
+        const TcRow r = tc_row<6>(p, 0, mt, row);
+#pragma unroll 2
+        for (uint32_t j = 0; j < 8; ++j)
+        {
+            const uint32_t m = part + 4u * j;
+            int e_u = 0, e_v = 0;
+            if (r.ok)
+            {
+                tc_cbd_pair(p, pre, static_cast<uint32_t>(r.base + (static_cast<uint64_t>(m) << p.lo)), e_u, e_v);
+            }
+            const __half hu = __int2half_rn(e_u), hv = __int2half_rn(e_v);
+            st_shared_u16(sa + tc::operand_offset(row, m, tc_rows), *reinterpret_cast<const uint16_t*>(&hu));
+            st_shared_u16(sa + tc::operand_offset(row, m + 32u, tc_rows), *reinterpret_cast<const uint16_t*>(&hv));
+        }
+    }
+
+    // p.images: the eight images of the block (split s at s * tc_wide_b_bytes);
+    // p.tiles: the row tiles (rows = batch << lo, lo = log N - 6); the output
+    // is digit planes (stride p.elements)
+    template<int DC>
+    __global__ void __launch_bounds__(512 + 32, 1) tc_wide_kernel(const TcGroupParams p)
+    {
+        constexpr int tc_threads = 512;
+        extern __shared__ __align__(1024) uint8_t tc_smem[];
+        uint8_t* sb = tc_smem;                              // two image buffers
+        uint8_t* sa = tc_smem + 2 * tc_wide_b_bytes;        // the digit tile
+        uint64_t* bars = reinterpret_cast<uint64_t*>(sa + tc_wide_a_bytes);
+        uint64_t* bar_b = bars;            // [2] image landed
+        uint64_t* bar_bfree = bars + 2;    // [2] MMAs reading the image complete (commit)
+        uint64_t* bar_a_full = bars + 4;   // tile stored (one arrival per worker)
+        uint64_t* bar_a_empty = bars + 5;  // all eight splits' MMAs of the tile complete (commit)
+        uint64_t* bar_acc_full = bars + 6;   // [2]
+        uint64_t* bar_acc_empty = bars + 8;  // [2] one arrival per worker
+        uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 10);
+        volatile uint32_t* abort_flag = tslot + 1;
+        static_assert(11 * sizeof(uint64_t) <= tc_wide_control, "control block");
+
+        const uint32_t tid = threadIdx.x;
+        const uint32_t warp = tid >> 5, lane = tid & 31u;
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+        const uint64_t t_begin = p.tiles * blockIdx.x / gridDim.x;
+        const uint64_t t_end = p.tiles * (blockIdx.x + 1) / gridDim.x;
+        const uint64_t count = t_end - t_begin;
+
+        if (tid == 0)
+        {
+            for (int b = 0; b < 2; ++b)
+            {
+                tc::mbar_init(&bar_b[b], 1);
+                tc::mbar_init(&bar_bfree[b], 1);
+                tc::mbar_init(&bar_acc_full[b], 1);
+                tc::mbar_init(&bar_acc_empty[b], tc_threads);
+            }
+            tc::mbar_init(bar_a_full, tc_threads);
+            tc::mbar_init(bar_a_empty, 1);
+            *abort_flag = 0;
+            tc::mbar_init_fence();
+        }
+        if (warp == 0)
+        {
+            tc::tmem_alloc(tslot, 512);
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        const uint32_t tmem = *tslot;
+
+        auto give_up = [&](uint32_t code) {
+            atomicExch(p.error, code);
+            *abort_flag = 1;
+        };
+
+        if (warp == tc_threads / 32)
+        {
+            // ------------------------------------------------ MMA and copies
+            if (lane == 0 && count)
+            {
+                constexpr uint32_t idesc = tc::f16_instr_descriptor(tc_rows, 256);
+                constexpr uint32_t lbo_a = tc_rows / 8 * 128;
+                constexpr uint32_t lbo_b = 256 / 8 * 128;
+                const uint64_t total = count * tc_wide_splits;
+                uint32_t issued0 = 0, issued1 = 0, landed0 = 0, landed1 = 0;
+                auto copy = [&](uint32_t split) {
+                    const uint32_t buf = split & 1u;
+                    issued0 += buf == 0u ? 1u : 0u;
+                    issued1 += buf != 0u ? 1u : 0u;
+                    tc::mbar_arrive_expect_tx(&bar_b[buf], tc_wide_b_bytes);
+                    tc::bulk_g2s(sb + buf * tc_wide_b_bytes, p.images + static_cast<uint64_t>(split) * tc_wide_b_bytes,
+                                 tc_wide_b_bytes, &bar_b[buf]);
+                };
+                copy(0);
+                copy(1);
+                for (uint64_t i = 0; i < count && !*abort_flag; ++i)
+                {
+                    if (!tc::mbar_wait_sleep(bar_a_full, static_cast<uint32_t>(i & 1u), p.spin_limit, 200u))
+                    {
+                        give_up(14);
+                        break;
+                    }
+                    for (uint32_t s = 0; s < static_cast<uint32_t>(tc_wide_splits); ++s)
+                    {
+                        const uint64_t j = i * tc_wide_splits + s;
+                        const uint32_t buf = static_cast<uint32_t>(j & 1u);
+                        const uint32_t par = static_cast<uint32_t>((j >> 1) & 1u);
+                        if (!tc::mbar_wait(&bar_b[buf], par, p.spin_limit))
+                        {
+                            give_up(11);
+                            break;
+                        }
+                        landed0 += buf == 0u ? 1u : 0u;
+                        landed1 += buf != 0u ? 1u : 0u;
+                        if (j >= 2 && !tc::mbar_wait(&bar_acc_empty[buf], static_cast<uint32_t>(((j - 2) >> 1) & 1u),
+                                                     p.spin_limit))
+                        {
+                            give_up(15);
+                            break;
+                        }
+                        tc::fence_after_sync();
+                        const uint32_t a0 = tc::smem_u32(sa);
+                        const uint32_t b0 = tc::smem_u32(sb + buf * tc_wide_b_bytes);
+#pragma unroll
+                        for (int ks = 0; ks < tc_wide_r / 16; ++ks)
+                        {
+                            tc::mma_f16(tmem + buf * 256u, tc::smem_descriptor(a0 + ks * 2 * lbo_a, lbo_a, 128),
+                                        tc::smem_descriptor(b0 + ks * 2 * lbo_b, lbo_b, 128), idesc, ks > 0);
+                        }
+                        tc::mma_commit(&bar_acc_full[buf]);
+                        tc::mma_commit(&bar_bfree[buf]);
+                        if (s + 1 == static_cast<uint32_t>(tc_wide_splits))
+                        {
+                            tc::mma_commit(bar_a_empty);
+                        }
+                        if (j + 2 < total)
+                        {
+                            // the image buffer is free once these MMAs complete
+                            if (!tc::mbar_wait(&bar_bfree[buf], par, p.spin_limit))
+                            {
+                                give_up(12);
+                                break;
+                            }
+                            copy((s + 2u) % static_cast<uint32_t>(tc_wide_splits));
+                        }
+                    }
+                }
+                if (*abort_flag)
+                {
+                    // copies still in flight land before the shared memory is released
+                    if (issued0 > landed0)
+                    {
+                        tc::mbar_wait(&bar_b[0], landed0 & 1u, p.spin_limit);
+                    }
+                    if (issued1 > landed1)
+                    {
+                        tc::mbar_wait(&bar_b[1], landed1 & 1u, p.spin_limit);
+                    }
+                }
+            }
+        }
+        else
+        {
+            // ------------------------------------------------ workers
+            asm volatile("griddepcontrol.wait;" ::: "memory");
+            const ChachaPre pre = chacha_pre(p.rng);
+            for (uint64_t i = 0; i < count; ++i)
+            {
+                const uint32_t mt = static_cast<uint32_t>(t_begin + i);
+                if (i > 0)
+                {
+                    // the previous tile's MMAs no longer read the digit tile
+                    uint32_t ok = 1;
+                    if (lane == 0)
+                    {
+                        ok = tc::mbar_wait_sleep(bar_a_empty, static_cast<uint32_t>((i - 1) & 1u), p.spin_limit);
+                    }
+                    if (!__shfl_sync(0xffffffffu, ok, 0))
+                    {
+                        give_up(16);
+                        break;
+                    }
+                }
+                tc_store_cbd_wide(p, pre, sa, mt, tid);
+                tc::fence_proxy_async();
+                mbar_arrive(bar_a_full);
+                bool stop = false;
+                for (uint32_t s = 0; s < static_cast<uint32_t>(tc_wide_splits); ++s)
+                {
+                    const uint64_t j = i * tc_wide_splits + s;
+                    const uint32_t buf = static_cast<uint32_t>(j & 1u);
+                    uint32_t ok = 1;
+                    if (lane == 0)
+                    {
+                        ok = tc::mbar_wait_sleep(&bar_acc_full[buf], static_cast<uint32_t>((j >> 1) & 1u),
+                                                 p.spin_limit);
+                    }
+                    if (!__shfl_sync(0xffffffffu, ok, 0))
+                    {
+                        give_up(17);
+                        stop = true;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const TcCursor cur{s, mt, 0};
+                    tc_epilogue<DC, tc_wide_r, tc_out_digits, tc_wide_splits, false, false, true, false>(
+                        p, tmem + buf * 256u, cur, warp, lane);
+                    tc::fence_before_sync();
+                    mbar_arrive(&bar_acc_empty[buf]);
+                    if (*abort_flag)
+                    {
+                        stop = true;
+                        break;
+                    }
+                }
+                if (stop || *abort_flag)
+                {
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        if (*abort_flag && tid == 0)
+        {
+            // give in-flight MMAs a bounded chance to land before the memory is released
+            tc::mbar_wait(&bar_bfree[0], 0, p.spin_limit);
+            tc::mbar_wait(&bar_bfree[0], 1, p.spin_limit);
+            tc::mbar_wait(&bar_bfree[1], 0, p.spin_limit);
+            tc::mbar_wait(&bar_bfree[1], 1, p.spin_limit);
+        }
+        __syncthreads();
+        tc::fence_after_sync();
+        if (warp == 0)
+        {
+            tc::tmem_dealloc(tmem, 512);
+        }
+    }
+
     // ------------------------------------------------------------- constants
 
     struct TcGenParams
@@ -1294,6 +1557,50 @@ namespace hmpc_gb300
             {
                 p.gx[((h * r + k) * r + i) * L + j] = out[j];
             }
+        }
+    }
+
+    // The wide group's 64 x 64 matrix over Z_q from the first two three-stage
+    // groups of the forward transform: the second applies B_kh (block kh =
+    // the element's top three bits, already mixed by the first) to the low
+    // three bits, the first A to the top three, so G6[(kh, kl)][(ih, il)] =
+    // B_kh[kl][il] * A[kh][ih], optionally times a scale (all Montgomery).
+    struct TcCombineParams
+    {
+        const uint32_t* gx_a;   // [1][8][8][L]
+        const uint32_t* gx_b;   // [8][8][8][L]
+        const uint32_t* scale;  // [L] Montgomery form, or nullptr
+        uint32_t* gx;           // [1][64][64][L]
+    };
+
+    template<int L>
+    __global__ void tc_combine6_kernel(const TcCombineParams p, const Modulus<L> m)
+    {
+        const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+        if (id >= 64u * 64u)
+        {
+            return;
+        }
+        const uint32_t k = id / 64u, i = id % 64u;
+        const uint32_t kh = k >> 3, kl = k & 7u, ih = i >> 3, il = i & 7u;
+        uint32_t a[L], b[L], v[L];
+        for (int j = 0; j < L; ++j)
+        {
+            a[j] = p.gx_a[((kh * 8u) + ih) * L + j];
+            b[j] = p.gx_b[((kh * 8u + kl) * 8u + il) * L + j];
+        }
+        mont_mul<L>(v, b, a, m);
+        if (p.scale)
+        {
+            for (int j = 0; j < L; ++j)
+            {
+                a[j] = p.scale[j];
+            }
+            mont_mul<L>(v, v, a, m);
+        }
+        for (int j = 0; j < L; ++j)
+        {
+            p.gx[static_cast<uint64_t>(id) * L + j] = v[j];
         }
     }
 
