@@ -304,12 +304,16 @@ namespace
 
     // whether a forward plan starts with two three-stage groups and has at
     // least two more after them (the wide group replaces the first two)
-    bool wide_plan(const TcTables* tt)
+    bool wide_plan(const std::vector<TcGroupPlan>& groups)
     {
         // the second group must write plain planes (not the blocked runs of a
         // group before the last)
-        return tt->groups.size() >= 4 && tt->groups[0].g == 3 && tt->groups[1].g == 3 &&
-               (tt->groups[1].layout & 2) == 0;
+        return groups.size() >= 4 && groups[0].g == 3 && groups[1].g == 3 && (groups[1].layout & 2) == 0;
+    }
+
+    bool wide_plan(const TcTables* tt)
+    {
+        return wide_plan(tt->groups);
     }
 
     // the wide group's images: unscaled, and scaled by p (nullptr: not needed)
@@ -649,6 +653,30 @@ namespace hmpc_gb300::detail
         {
             return rc;
         }
+        if (cbd && !small && !inverse && wide_plan(tt))
+        {
+            // the first six stages in one wide group into buffer 1, then the
+            // groups from the third on
+            if (int rc = prepare_wide(ctx, mod, n, tt, nullptr))
+            {
+                return rc;
+            }
+            if (int rc = run.wide(tt->wide_cbd, digits + w * elements, elements, batch, vx2))
+            {
+                return rc;
+            }
+            for (size_t j = 2; j < stages; ++j)
+            {
+                const uint32_t* in = digits + (((j - 1) & 1u) ? w * elements : 0);
+                uint32_t* o = j + 1 == stages ? out : digits + ((j & 1u) ? w * elements : 0);
+                if (int rc = run.group(j, in, o, elements, batch, tc_in_digits, 0, nullptr, elements, true))
+                {
+                    return rc;
+                }
+            }
+            nonce_add(ctx->nonce, elements);
+            return HMPC_OK;
+        }
         const int first_kind = cbd ? (small ? tc_in_small : tc_in_cbd) : tc_in_limbs;
         for (size_t j = 0; j < stages; ++j)
         {
@@ -871,7 +899,20 @@ namespace hmpc_gb300::detail
         out->launches = static_cast<uint32_t>(groups.size());
         out->bytes = 0.0;
         out->flops = 0.0;
-        for (size_t j = 0; j < groups.size(); ++j)
+        size_t first = 0;
+        if (kind == producer_cbd && wide_plan(groups))
+        {
+            // the wide group: digit planes written, eight images read, eight
+            // N = 256 products of K = 64 per 128-row tile
+            const uint64_t rows = batch << (log_n - 6);
+            const double tiles = static_cast<double>((rows + tc_rows - 1) / tc_rows);
+            out->launches -= 1;
+            out->bytes += elements * 4.0 * groups[1].shape.w_out +
+                          static_cast<double>(tc_wide_splits) * tc_wide_b_bytes;
+            out->flops += tiles * tc_wide_splits * 2.0 * tc_rows * 256.0 * tc_wide_r;
+            first = 2;
+        }
+        for (size_t j = first; j < groups.size(); ++j)
         {
             TcShapeInfo shape = groups[j].shape;
             const bool cbd = j == 0 && kind == producer_cbd;
