@@ -51,7 +51,7 @@ CONFIG = {
 # kernel: the mean over the five tc_group_kernel launches of one fused CBD(10)
 # transform of 256 x 2^15, from the one-pass ncu capture summarised in
 # profiles/tc_group_kernel_cbd_n32768_L8.md (sum of its five launches / 5)
-DOMINANT_TRAFFIC_BYTES = 628.0e6
+DOMINANT_TRAFFIC_BYTES = 648.0e6
 DOMINANT_TRAFFIC_PROFILE = "profiles/tc_group_kernel_cbd_n32768_L8.md"
 
 
