@@ -216,6 +216,8 @@ struct hmpc_modulus
             cudaFree(kv.second.images);
             cudaFree(kv.second.first_cbd);
             cudaFree(kv.second.first_small);
+            cudaFree(kv.second.wide_cbd);
+            cudaFree(kv.second.wide_cbd_p);
         }
     }
 
