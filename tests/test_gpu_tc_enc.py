@@ -34,7 +34,7 @@ Q_224 = 0xE9E9C9C7700173EE913AE1871AE48451A42CE7E731BC0F8A00C20001
 
 
 @pytest.mark.parametrize("qv,pv", [(Q_256, P_64), (Q_128, P_64), (Q_256, P_32), (Q_192, P_64), (Q_224, P_32)])
-@pytest.mark.parametrize("n,batch", [(1 << 12, 3), (64, 5), (32, 2), (1 << 10, 130)])
+@pytest.mark.parametrize("n,batch", [(1 << 12, 3), (64, 5), (32, 2), (1 << 10, 130), (1 << 16, 1)])
 @pytest.mark.parametrize("plaintext_ntt", [False, True])
 def test_three_transform_encryption_matches_oracle(queue, oracle, qv, pv, n, batch, plaintext_ntt, cpu_threads):
     om_q, om_p = oracle.Modulus(qv), oracle.Modulus(pv)

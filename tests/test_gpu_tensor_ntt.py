@@ -84,6 +84,25 @@ def test_fused_cbd_matches_oracle(queue, oracle, q, vx2, cpu_threads):
     assert np.array_equal(y.numpy(), ref)
 
 
+@pytest.mark.parametrize("q", [Q_256, Q_128, Q_192])
+@pytest.mark.parametrize("n,batch", [(1 << 10, 1), (1 << 10, 3), (1 << 16, 1), (1 << 16, 2)])
+@pytest.mark.parametrize("vx2", [1, 64])
+def test_wide_first_group_edges(queue, oracle, q, n, batch, vx2, cpu_threads):
+    """the first six stages as one group: the smallest and largest degrees it
+    covers (four groups at 2^10, the wide one then 3 + 1 stages; 2^16), a
+    single polynomial (fewer rows than one 128-row tile), both ends of 2V"""
+    om, gm = oracle.Modulus(q), queue.modulus(q)
+    tensor_plan(gm, n, batch)
+    nonce = [0x7FFFFFFF, 0xFFFFFFFF, 2]
+    queue.nonce = nonce
+    before = queue.launches
+    y = queue.ntt_centered_binomial(gm, n, (batch,), vx2)
+    assert queue.launches - before == groups(n) - 1  # the wide group replaces the first two
+    assert queue.nonce == oracle.nonce_add(nonce, n * batch)
+    ref = oracle.ntt(om, n, batch, sampler="cbd", variance_x2=vx2, key=KEY, nonce=nonce, threads=cpu_threads)
+    assert np.array_equal(y.numpy(), ref)
+
+
 def test_full_size_bgv_transform(queue, oracle, cpu_threads):
     """the bench's transform shape: 2^15 coefficients, q 256-bit, a batch
     spanning several 128-row tiles per constant matrix"""
