@@ -603,6 +603,14 @@ namespace hmpc_gb300::detail
             p.rng = ctx->rng();
             p.vx2 = vx2;
             p.nw = (2 * vx2 + 31) / 32;
+            // dependent launch: its constants were built before this call's
+            // first launch, and its workers wait for the kernel before it
+            // (ordinary launches while the stream is being captured)
+            cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+            p.dependent = cudaStreamIsCapturing(stream, &capture) == cudaSuccess &&
+                                  capture == cudaStreamCaptureStatusNone
+                              ? 1u
+                              : 0u;
             const unsigned grid =
                 static_cast<unsigned>(std::min<uint64_t>(p.tiles, static_cast<uint64_t>(ctx->sm_count)));
             cudaError_t e = k->wide(p, grid, stream);

@@ -224,8 +224,17 @@ namespace hmpc_gb300
             {
                 return configured;
             }
-            tc_wide_kernel<DC><<<grid, 512 + 32, tc_wide_smem, stream>>>(p);
-            return cudaGetLastError();
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(grid);
+            cfg.blockDim = dim3(512 + 32);
+            cfg.dynamicSmemBytes = tc_wide_smem;
+            cfg.stream = stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = p.dependent ? 1u : 0u;
+            return cudaLaunchKernelEx(&cfg, tc_wide_kernel<DC>, p);
         }
 
         const TcKernels table = {DC, group, shape, gen, expand, combine6, wide};
