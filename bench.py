@@ -1055,6 +1055,24 @@ def main():
     barrier()
     e2e_ms = max_over_ranks(e_start.elapsed_time(e_stop), world, device="cuda")
     e2e_value = whole_job_rate(BATCH, world, args.steps, e2e_ms)
+    # the same loop for about a second, with clock samples (copies beside
+    # kernels: where a box runs them slowly, its clocks and throttle reasons
+    # show whether the GPU was held back meanwhile)
+    e2e_sustained = None
+    if not args.no_sustained:
+        count = max(args.steps, int(1000.0 / max(e2e_ms / args.steps, 1e-3)) + 1)
+        barrier()
+        es_start, es_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as es_clocks:
+            es_start.record(stream)
+            copy_in.wait_stream(stream)
+            e2e_run(count)
+            stream.wait_stream(copy_out)
+            es_stop.record(stream)
+            barrier()
+        es_ms = max_over_ranks(es_start.elapsed_time(es_stop), world, device="cuda")
+        e2e_sustained = {"steps": count, "value": whole_job_rate(BATCH, world, count, es_ms),
+                         "clocks": es_clocks.summary()}
     last = sets[(args.steps - 1) % 2]
     host_c0, host_c1 = last["c0"], last["c1"]
     # check the e2e result once: decrypting the copied-back ciphertext gives the messages
@@ -1120,6 +1138,7 @@ def main():
                 "link_gbs": link,
                 "copy_bound": BATCH / copy_s,
                 "host_numa": host_numa,
+                "sustained": e2e_sustained,
             },
             "gpu_launches": launches,
             "roofline": roofline,
