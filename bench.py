@@ -10,7 +10,8 @@ the sizes of the BGV configuration).  Metric: encryptions per second.
   value  -- inputs resident in HBM, device-timed with CUDA events
   e2e    -- the same step through the public API with the plaintexts copied
             from pinned host memory and both ciphertext components copied
-            back to pinned host memory inside the timed region
+            back to pinned host memory inside the timed region, over about a
+            second of steps (the K-step window too: e2e.k_steps)
   --impl reference -- the reference algorithm on the host cores (the CPU
             oracle: the reference's SYCL build cannot be compiled here)
 
@@ -1129,16 +1130,23 @@ def main():
             "dtype": "u32 limbs (exact modular integer arithmetic)",
             "data": "synthetic (seeded ChaCha20 keys, noise and messages)",
             "config": CONFIG,
+            # the end-to-end value is the one-second loop's: the host link of
+            # these boxes slows down transiently, so a K-step window of about
+            # 60 ms measured anywhere from 40k to 76k/s on one box while the
+            # one-second loop stayed within 62-70k/s (the K-step figure is kept)
             "e2e": {
-                "value": e2e_value,
+                "value": e2e_sustained["value"] if e2e_sustained else e2e_value,
                 "unit": "encryptions/s",
+                "window": (f"{e2e_sustained['steps']} steps (about a second)" if e2e_sustained
+                           else f"{args.steps} steps"),
                 "h2d_bytes_per_step": host_msgs.numel() * 4,
                 "d2h_bytes_per_step": (host_c0.numel() + host_c1.numel()) * 4,
                 "decrypts_ok": ok,
+                "k_steps": {"steps": args.steps, "value": e2e_value},
+                "clocks": e2e_sustained["clocks"] if e2e_sustained else None,
                 "link_gbs": link,
                 "copy_bound": BATCH / copy_s,
                 "host_numa": host_numa,
-                "sustained": e2e_sustained,
             },
             "gpu_launches": launches,
             "roofline": roofline,
